@@ -1,0 +1,238 @@
+/*
+ * tn_mps.h -- C ABI of the GB300 Schmidt-form (Gamma-Lambda) MPS trajectory engine.
+ *
+ * Drop-in boundary for whooie/tensor-net's `MPS<Q, C64>` trajectory path
+ * (tensor-net/lib/mps.rs).  The reference is Rust and has no FFI of its own; the
+ * entry points below are what a Rust `extern "C"` binding of that API binds,
+ * one per inherent method it replaces (file:line cited beside each).
+ *
+ * Conventions (mirroring the reference):
+ *  - complex numbers cross the ABI as interleaved (re, im) float64 pairs;
+ *    matrices are row-major, so a 4x4 gate is 32 doubles, a 2x2 gate 8;
+ *  - an out-of-range site/bond is a silent no-op for mutators (TN_OK) and
+ *    TN_NONE for queries, as the reference returns `Ok(self)` / `None`;
+ *  - a wrongly shaped operator is TN_ERR_OPERATOR_SHAPE (MPSError::
+ *    OperatorIncompatibleShape, mps.rs:148-150);
+ *  - randomness is never drawn inside the library: measurements take a
+ *    caller-supplied uniform u in [0,1) in place of the reference's `rng.gen()`
+ *    (mps.rs:1433); outcome = first s with u < cumsum(p)_s, i.e. (u < p0) ? 0 : 1;
+ *  - one handle is one CUDA stream and is not thread-safe (the reference takes
+ *    `&mut self`); distinct handles may be used from distinct threads;
+ *  - host arrays passed in are read/written only during the call.
+ *
+ * Device state lives in HBM for the handle's lifetime: Gamma tensors in
+ * fixed-capacity slots, Lambda vectors in float64, bond dimensions on the
+ * device (truncation is decided on the GPU with no host round trip).
+ */
+#ifndef TN_MPS_H
+#define TN_MPS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (MPSError, mps.rs:126-154, plus device-side errors) ---- */
+enum {
+    TN_OK = 0,
+    TN_NONE = 1,                     /* reference returns None (out-of-range query) */
+    TN_ERR_EMPTY_SYSTEM = -1,        /* MPSError::EmptySystem            mps.rs:131 */
+    TN_ERR_INVALID_QNUM = -2,        /* MPSError::InvalidQuantumNumber   mps.rs:136 */
+    TN_ERR_UNPHYSICAL_INDEX = -3,    /* MPSError::UnphysicalIndex        mps.rs:141 */
+    TN_ERR_STATE_SHAPE = -4,         /* MPSError::StateIncompatibleShape mps.rs:146 */
+    TN_ERR_OPERATOR_SHAPE = -5,      /* MPSError::OperatorIncompatibleShape mps.rs:150 */
+    TN_ERR_INVALID_ARG = -6,         /* null pointer, bad enum, bad size */
+    TN_ERR_CUDA = -7,                /* a CUDA runtime call failed */
+    TN_ERR_OOM = -8,                 /* device or pinned-host allocation failed */
+    TN_ERR_CAPACITY = -9,            /* a bond would exceed the handle's chi capacity */
+    TN_ERR_NOT_CONVERGED = -10,      /* Jacobi SVD hit its sweep limit */
+    TN_ERR_PROB_SUM = -11,           /* |p0 + p1 - 1| above tolerance at a measurement */
+    TN_ERR_NO_DEVICE = -12           /* no CUDA device / kernels cannot run */
+};
+
+/* Truncation rule.  mps.rs:157-166 `BondDim` is Const(r) or Cutoff(eps);
+ * `trunc = NULL` is the reference's `None` (cutoff at f64::EPSILON).
+ * TN_TRUNC_BOTH is the combined rule used by the benchmark workloads:
+ * rank = max(1, min(chi_max, #{leading s_j normal and > |cutoff|})). */
+typedef enum {
+    TN_TRUNC_NONE = 0,
+    TN_TRUNC_CONST = 1,
+    TN_TRUNC_CUTOFF = 2,
+    TN_TRUNC_BOTH = 3
+} tn_trunc_mode;
+
+typedef struct {
+    int32_t mode;       /* tn_trunc_mode */
+    uint32_t chi_max;   /* CONST / BOTH */
+    double cutoff;      /* CUTOFF / BOTH */
+} tn_trunc;
+
+/* Arithmetic of the device path.  F64: complex128 Gamma, float64 Jacobi SVD
+ * (the plain path).  MIXED: complex64 Gamma and theta, float32 Jacobi sweeps
+ * accumulated in float32, float64 Lambda, renormalisation, rank decision,
+ * probabilities and entropies. */
+typedef enum {
+    TN_PREC_F64 = 0,
+    TN_PREC_MIXED = 1
+} tn_precision;
+
+typedef struct tn_mps tn_mps;
+typedef struct tn_batch tn_batch;
+
+const char *tn_status_string(int status);
+/* Text of the last CUDA failure seen by the calling thread ("" if none). */
+const char *tn_last_error(void);
+
+/* Library / device information.  Fills `name` (cap bytes) with the GPU name and
+ * `sm_count` with its SM count; TN_ERR_NO_DEVICE without a GPU. */
+int tn_device_info(char *name, uint32_t cap, uint32_t *sm_count);
+
+/* ======================= single state: MPS<Q, C64> ======================= */
+
+/* MPS::new_qubits(n, trunc) (mps.rs:2033-2039 -> MPS::new, mps.rs:370-391):
+ * |0...0>, every Gamma 1x2x1 with [0,0,0] = 1, every Lambda = [1].
+ * chi_cap bounds every bond dimension (device slot size); 0 picks chi_max for
+ * CONST/BOTH, else min(2^(n/2), 256).  n == 0 -> TN_ERR_EMPTY_SYSTEM. */
+int tn_mps_new_qubits(uint32_t n, const tn_trunc *trunc, int32_t precision,
+                      uint32_t chi_cap, tn_mps **out);
+int tn_mps_free(tn_mps *m);
+/* #[derive(Clone)] (mps.rs:338). */
+int tn_mps_clone(const tn_mps *m, tn_mps **out);
+int tn_mps_n(const tn_mps *m, uint32_t *n);
+/* get_trunc / set_trunc (mps.rs:1216-1221); set_trunc(NULL) = None. */
+int tn_mps_get_trunc(const tn_mps *m, tn_trunc *out);
+int tn_mps_set_trunc(tn_mps *m, const tn_trunc *trunc);
+
+/* apply_unitary1 (mps.rs:1298-1314): op is rows x cols complex, must be 2x2. */
+int tn_mps_apply_unitary1(tn_mps *m, uint32_t k, const double *op,
+                          uint32_t rows, uint32_t cols);
+/* apply_unitary2 (mps.rs:1332-1387): op is rows x cols complex, must be 4x4,
+ * acting on the fused pair index s_k*2 + s_{k+1}. */
+int tn_mps_apply_unitary2(tn_mps *m, uint32_t k, const double *op,
+                          uint32_t rows, uint32_t cols);
+
+/* probs (mps.rs:1071-1076): out[0..2]. */
+int tn_mps_probs(const tn_mps *m, uint32_t k, double out[2]);
+/* prob (mps.rs:1138-1143). */
+int tn_mps_prob(const tn_mps *m, uint32_t k, uint32_t p, double *out);
+
+/* measure_prob (mps.rs:1479-1489): sample with uniform u, project, full
+ * refactor sweep (mps.rs:894-897). */
+int tn_mps_measure_prob(tn_mps *m, uint32_t k, double u,
+                        int32_t *outcome, double *prob);
+/* measure_postsel_prob (mps.rs:1501-1510). */
+int tn_mps_measure_postsel_prob(tn_mps *m, uint32_t k, uint32_t p, double *prob);
+
+/* apply_meas_prob_layer (mps.rs:2206-2252) / measure_prob_layer (1552-1582).
+ * ks[nk] targets in any order; out-of-range ones are dropped, duplicates
+ * removed (first kept), the rest sorted ascending.  `posts` may be NULL (all
+ * Meas::Rand); posts[i] >= 0 makes target i a Meas::Proj post-selection.
+ * us[j] is the uniform of the j-th surviving target in ascending order (the
+ * order the reference draws from its rng).  Outputs (capacity nk each):
+ * out_ks, outcomes, probs; *n_out = number of surviving targets. */
+int tn_mps_apply_meas_prob_layer(tn_mps *m, const uint32_t *ks, uint32_t nk,
+                                 const int32_t *posts, const double *us,
+                                 uint32_t *out_ks, int32_t *outcomes, double *probs,
+                                 uint32_t *n_out);
+
+/* circuit::apply_bilayer (circuit.rs:624-659) with Uni::Mat 4x4 gates:
+ * gates[ng*32] applied at gate_ks[ng] in order (apply_unitary2), then one
+ * apply_meas_prob_layer over meas_ks/us (posts NULL).  One device launch. */
+int tn_mps_apply_bilayer(tn_mps *m, const uint32_t *gate_ks, const double *gates,
+                         uint32_t ng, const uint32_t *meas_ks, uint32_t nm,
+                         const double *us, uint32_t *out_ks, int32_t *outcomes,
+                         double *probs, uint32_t *n_out);
+
+/* entropy_vn (mps.rs:1251-1261), float64 on the device. */
+int tn_mps_entropy_vn(const tn_mps *m, uint32_t b, double *out);
+/* entropy_ry_schmidt (mps.rs:1268-1282). */
+int tn_mps_entropy_ry_schmidt(const tn_mps *m, double a, uint32_t b, double *out);
+/* bond_dim / max_bond_dim (mps.rs:1224-1245). */
+int tn_mps_bond_dim(const tn_mps *m, uint32_t b, uint32_t *out);
+int tn_mps_max_bond_dim(const tn_mps *m, uint32_t *out);
+/* Lambda on bond b (the reference's svals[b], mps.rs:352-353). */
+int tn_mps_svals(const tn_mps *m, uint32_t b, double *out, uint32_t cap, uint32_t *len);
+/* Gamma of site k in the reference layout (chi_{k-1}, 2, chi_k), row-major,
+ * interleaved complex128 (mps.rs:344-349).  dims[3] receives the shape. */
+int tn_mps_export_gamma(const tn_mps *m, uint32_t k, double *out, uint64_t cap,
+                        uint32_t dims[3]);
+/* contract (mps.rs:794-798): the dense 2^n state vector, interleaved
+ * complex128, s_0 most significant; n <= 24. */
+int tn_mps_contract(const tn_mps *m, double *out, uint64_t cap);
+/* Device-side error word accumulated by this handle's kernels (0 if none);
+ * cleared on read. */
+int tn_mps_device_status(tn_mps *m, int32_t *status);
+
+/* ==================== batch of trajectories (batching) ==================== */
+
+/* Many independent trajectories, each its own MPS (own n, truncation), all
+ * resident on the device; one persistent launch advances every active
+ * trajectory by one brickwork layer (gates, measurement layer with its
+ * refactor sweep, half-chain entropy).  Results per trajectory do not depend
+ * on which other trajectories share the launch. */
+int tn_batch_create(uint32_t ntraj, const uint32_t *ns, const tn_trunc *truncs,
+                    int32_t precision, const uint32_t *chi_caps, tn_batch **out);
+int tn_batch_free(tn_batch *b);
+/* Re-initialise slot t to |0...0> with a new n/trunc (n and chi must fit the
+ * slot's allocation); used by the serving loop to reuse slots. */
+int tn_batch_reset(tn_batch *b, uint32_t t, uint32_t n, const tn_trunc *trunc);
+
+/* One brickwork layer for the trajectories listed in `trajs[nt]`:
+ * trajectory trajs[i] applies gates gate_off[i]..gate_off[i+1]-1 (sites
+ * gate_ks[], 4x4 complex128 gates[32 each]) then measures sites
+ * meas_off[i]..meas_off[i+1]-1 (meas_ks[] sorted ascending, unique, in range;
+ * uniforms us[]).  Outputs: outcomes[]/probs[] parallel to meas_ks, and
+ * entropy[i] = entropy_vn(n/2 - 1) after the layer.  Host arrays; the call
+ * copies them in, launches once, copies results back and synchronises. */
+int tn_batch_step(tn_batch *b, const uint32_t *trajs, uint32_t nt,
+                  const uint32_t *gate_off, const uint32_t *gate_ks, const double *gates,
+                  const uint32_t *meas_off, const uint32_t *meas_ks, const double *us,
+                  int32_t *outcomes, double *probs, double *entropy);
+
+/* Same layer, inputs already in device memory (pointers from tn_batch_device_inputs);
+ * no host copies, no synchronisation (stream-ordered on the batch stream). */
+int tn_batch_device_inputs(tn_batch *b, uint32_t max_gates, uint32_t max_meas,
+                           void **d_trajs, void **d_gate_off, void **d_gate_ks,
+                           void **d_gates, void **d_meas_off, void **d_meas_ks,
+                           void **d_us, void **d_outcomes, void **d_probs,
+                           void **d_entropy);
+int tn_batch_step_device(tn_batch *b, uint32_t nt);
+int tn_batch_synchronize(tn_batch *b);
+/* Per-trajectory queries (same meaning as the tn_mps_* ones). */
+int tn_batch_bond_dims(tn_batch *b, uint32_t t, uint32_t *out, uint32_t cap);
+int tn_batch_svals(tn_batch *b, uint32_t t, uint32_t bond, double *out, uint32_t cap,
+                   uint32_t *len);
+int tn_batch_device_status(tn_batch *b, int32_t *status);
+/* Device bytes held by slot t (its footprint for admission control). */
+int tn_batch_slot_bytes(tn_batch *b, uint32_t t, uint64_t *bytes);
+/* Stream the batch launches on (a cudaStream_t), for callers that time with
+ * CUDA events. */
+int tn_batch_stream(tn_batch *b, void **stream);
+
+/* ======================= seeded synthetic inputs ======================= */
+
+/* gate::haar(2, rng) (gate.rs:888-909) given the Ginibre sample z (4x4
+ * complex128, row-major, interleaved): QR, then column j divided by
+ * r_jj/|r_jj|.  Host code, float64. */
+int tn_haar_u4(const double *z, double *out);
+
+/* Counter-based generator of one brickwork layer of one trajectory
+ * (circuit.rs:558-584 haar_layer + uniform_meas, gate positions
+ * workspace/lib/haar.rs:285: offset = layer odd): all values are pure
+ * functions of (seed, traj, layer, site, purpose).  gates[] needs room for
+ * 32*(n/2) doubles, gate_ks/meas_ks/us for n entries.  Host code. */
+int tn_gen_layer(uint64_t seed, uint64_t traj, uint32_t layer, uint32_t n, double p,
+                 uint32_t *gate_ks, double *gates, uint32_t *ng,
+                 uint32_t *meas_ks, double *us, uint32_t *nm);
+
+/* The Ginibre sample (4x4 complex128) behind the gate at `site` of a layer
+ * produced by tn_gen_layer, for checking tn_haar_u4 against another QR. */
+int tn_gen_ginibre(uint64_t seed, uint64_t traj, uint32_t layer, uint32_t site, double *z);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TN_MPS_H */

@@ -1,0 +1,16 @@
+"""GB300-native Schmidt-form (Gamma-Lambda) MPS trajectory engine.
+
+A drop-in for the ``MPS<Q, C64>`` trajectory path of whooie/tensor-net: the
+state lives in HBM, every bond operation (theta contraction, Jacobi SVD,
+truncation, Lambda renormalisation), measurement and entropy read runs in
+hand-written sm_103a kernels behind the C ABI of ``include/tn_mps.h``.
+This package is the host-side mirror of the reference API over that ABI.
+"""
+from . import build
+from ._lib import STATUS, TnError, lib, library_path
+from .batch import Batch
+from .inputs import gen_layer, gen_trajectory, ginibre, haar_u4
+from .mps import MPS, Trunc
+
+__all__ = ["MPS", "Trunc", "Batch", "TnError", "STATUS", "lib", "library_path", "build",
+           "gen_layer", "gen_trajectory", "ginibre", "haar_u4"]

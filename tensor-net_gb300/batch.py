@@ -1,0 +1,122 @@
+"""Batch of independent trajectories over ``tn_batch_*`` (one persistent
+launch per brickwork layer for every listed trajectory)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from .mps import PRECISIONS, Trunc
+
+
+class Batch:
+    def __init__(self, ns, truncs=None, precision: str = "mixed", chi_caps=None):
+        self._lib = L.lib()
+        ns = np.ascontiguousarray(np.asarray(ns, dtype=np.uint32))
+        self.ntraj = int(ns.size)
+        self.ns = ns.copy()
+        tarr = None
+        if truncs is not None:
+            tarr = (L.tn_trunc * self.ntraj)(*[t.c() for t in truncs])
+        caps = None if chi_caps is None else np.ascontiguousarray(np.asarray(chi_caps, dtype=np.uint32))
+        self._h = C.c_void_p()
+        L.check(self._lib.tn_batch_create(self.ntraj, L.uptr(ns), tarr, PRECISIONS[precision], L.uptr(caps),
+                                          C.byref(self._h)), "tn_batch_create")
+
+    def close(self):
+        if self._h:
+            self._lib.tn_batch_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reset(self, t: int, n: int, trunc: Trunc | None):
+        tr = C.byref(trunc.c()) if trunc is not None else None
+        L.check(self._lib.tn_batch_reset(self._h, int(t), int(n), tr), "tn_batch_reset")
+        self.ns[t] = n
+
+    @staticmethod
+    def pack(trajs, layers):
+        """layers[i] = (gate_ks, gates[ng,4,4] complex, meas_ks sorted, us)."""
+        gate_off = [0]
+        meas_off = [0]
+        gks, gs, mks, uss = [], [], [], []
+        for (gk, g, mk, us) in layers:
+            gk = np.asarray(gk, dtype=np.uint32).reshape(-1)
+            gks.append(gk)
+            gs.append(np.asarray(g, dtype=np.complex128).reshape(-1, 4, 4))
+            mks.append(np.asarray(mk, dtype=np.uint32).reshape(-1))
+            uss.append(np.asarray(us, dtype=np.float64).reshape(-1))
+            gate_off.append(gate_off[-1] + gk.size)
+            meas_off.append(meas_off[-1] + mks[-1].size)
+        cat = lambda xs, dt: np.ascontiguousarray(np.concatenate(xs).astype(dt)) if xs else np.zeros(0, dt)
+        return dict(
+            trajs=np.ascontiguousarray(np.asarray(trajs, dtype=np.uint32)),
+            gate_off=np.asarray(gate_off, np.uint32), gate_ks=cat(gks, np.uint32),
+            gates=np.ascontiguousarray(np.concatenate(gs).view(np.float64).reshape(-1)) if gs else np.zeros(0),
+            meas_off=np.asarray(meas_off, np.uint32), meas_ks=cat(mks, np.uint32), us=cat(uss, np.float64))
+
+    def step_packed(self, pk):
+        nt = pk["trajs"].size
+        nm = int(pk["meas_off"][-1])
+        oc = np.zeros(max(nm, 1), np.int32)
+        pr = np.zeros(max(nm, 1), np.float64)
+        ent = np.zeros(max(nt, 1), np.float64)
+        z = np.zeros(1)
+        zu = np.zeros(1, np.uint32)
+        L.check(self._lib.tn_batch_step(
+            self._h, L.uptr(pk["trajs"]), nt, L.uptr(pk["gate_off"]),
+            L.uptr(pk["gate_ks"] if pk["gate_ks"].size else zu),
+            L.dptr(pk["gates"] if pk["gates"].size else z), L.uptr(pk["meas_off"]),
+            L.uptr(pk["meas_ks"] if pk["meas_ks"].size else zu), L.dptr(pk["us"] if pk["us"].size else z),
+            L.iptr(oc), L.dptr(pr), L.dptr(ent)), "tn_batch_step")
+        return oc[:nm], pr[:nm], ent[:nt]
+
+    def step(self, trajs, layers):
+        """Advance each listed trajectory by its layer; returns per-trajectory
+        lists of (k, outcome, prob) and the half-chain entropies."""
+        pk = self.pack(trajs, layers)
+        oc, pr, ent = self.step_packed(pk)
+        recs = []
+        mo = pk["meas_off"]
+        for i in range(len(trajs)):
+            recs.append([(int(pk["meas_ks"][j]), int(oc[j]), float(pr[j])) for j in range(mo[i], mo[i + 1])])
+        return recs, ent
+
+    def bond_dims(self, t: int):
+        n = int(self.ns[t])
+        out = np.zeros(max(1, n - 1), np.uint32)
+        s = L.check(self._lib.tn_batch_bond_dims(self._h, int(t), L.uptr(out), out.size), "bond_dims")
+        return None if s == L.TN_NONE else out[: n - 1]
+
+    def svals(self, t: int, b: int):
+        ln = L.u32()
+        s = L.check(self._lib.tn_batch_svals(self._h, int(t), int(b), None, 0, C.byref(ln)), "svals")
+        if s == L.TN_NONE:
+            return None
+        out = np.zeros(max(1, ln.value))
+        L.check(self._lib.tn_batch_svals(self._h, int(t), int(b), L.dptr(out), out.size, C.byref(ln)), "svals")
+        return out[: ln.value]
+
+    def device_status(self) -> int:
+        st = L.i32()
+        L.check(self._lib.tn_batch_device_status(self._h, C.byref(st)), "device_status")
+        return int(st.value)
+
+    def slot_bytes(self, t: int) -> int:
+        b = L.u64()
+        L.check(self._lib.tn_batch_slot_bytes(self._h, int(t), C.byref(b)), "slot_bytes")
+        return int(b.value)
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        L.check(self._lib.tn_batch_stream(self._h, C.byref(s)), "stream")
+        return int(s.value or 0)
+
+    def synchronize(self):
+        L.check(self._lib.tn_batch_synchronize(self._h), "synchronize")

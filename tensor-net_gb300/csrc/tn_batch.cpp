@@ -1,0 +1,482 @@
+// tn_batch.cpp -- batch of independent trajectories advanced one brickwork
+// layer per persistent launch (the reference runs trajectories one per rayon
+// thread, workspace/src/haar_coev_probs.rs:164; here they share one launch).
+//
+// Per step:  H2D of the packed layer inputs (one copy from pinned memory)
+//            -> k_compile (instruction lists on the device)
+//            -> k_run (persistent CTAs pull trajectories, most expensive first)
+//            -> D2H of outcomes / probabilities / entropies (one copy).
+// The device-input variant skips both copies and replays a captured CUDA
+// graph of compile + run.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "tn_internal.h"
+#include "tn_mps.h"
+
+using namespace tn;
+
+extern "C" const char *tn_last_error(void);
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(cudaError_t e, const char *what) {
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return TN_ERR_OOM;
+  return TN_ERR_CUDA;
+}
+
+#define CKB(call)                                   \
+  do {                                              \
+    cudaError_t e__ = (call);                       \
+    if (e__ != cudaSuccess) return fail(e__, #call); \
+  } while (0)
+
+uint32_t max_rank(uint32_t n) { return n / 2 >= 20 ? (1u << 20) : (1u << (n / 2)); }
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace
+
+struct tn_batch {
+  int prec = TN_PREC_MIXED;
+  uint32_t ntraj = 0;
+  cudaStream_t st = nullptr;
+  int sms = 1, bps = 1, grid_max = 1;
+  int maxcap = 1, maxn = 1, sortP = 1, pcap = 8;
+  std::vector<uint32_t> n_alloc, cap;
+  std::vector<TrajDev> h;
+  std::vector<size_t> slot_bytes;
+  void *arena = nullptr;
+  TrajDev *dtraj = nullptr;
+  int *dstatus = nullptr;
+  void *ws = nullptr;
+  size_t ws_stride = 0;
+  // step buffers: one packed device block + one pinned host block
+  void *dstep = nullptr, *hstep = nullptr;
+  size_t step_bytes = 0;
+  uint32_t step_nt = 0, step_ng = 0, step_nm = 0;
+  Instr *dprog = nullptr;
+  Item *ditems = nullptr;
+  int *dcounter = nullptr;
+  // device-input mode
+  void *din = nullptr;
+  uint32_t din_gates = 0, din_meas = 0;
+  std::map<uint32_t, cudaGraphExec_t> graphs;
+};
+
+namespace {
+
+// Packed per-step layout (same offsets on host and device).
+struct StepLayout {
+  size_t list, order, goff, gks, moff, mks, gates, us, outc, probs, ents, total, in_bytes, out_off;
+};
+
+StepLayout step_layout(uint32_t nt, uint32_t ng, uint32_t nm) {
+  StepLayout L{};
+  size_t p = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = p;
+    p = align256(p + bytes);
+    return o;
+  };
+  L.gates = take(sizeof(double) * 32 * std::max<uint32_t>(ng, 1));
+  L.us = take(sizeof(double) * std::max<uint32_t>(nm, 1));
+  L.list = take(sizeof(int) * std::max<uint32_t>(nt, 1));
+  L.order = take(sizeof(int) * std::max<uint32_t>(nt, 1));
+  L.goff = take(sizeof(int) * (nt + 1));
+  L.gks = take(sizeof(int) * std::max<uint32_t>(ng, 1));
+  L.moff = take(sizeof(int) * (nt + 1));
+  L.mks = take(sizeof(int) * std::max<uint32_t>(nm, 1));
+  L.in_bytes = p;
+  L.out_off = p;
+  L.outc = take(sizeof(int) * std::max<uint32_t>(nm, 1));
+  L.probs = take(sizeof(double) * std::max<uint32_t>(nm, 1));
+  L.ents = take(sizeof(double) * std::max<uint32_t>(nt, 1));
+  L.total = p;
+  return L;
+}
+
+int ensure_step(tn_batch *b, uint32_t nt, uint32_t ng, uint32_t nm) {
+  if (nt <= b->step_nt && ng <= b->step_ng && nm <= b->step_nm && b->dstep) return TN_OK;
+  for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);  // they point at the old buffers
+  b->graphs.clear();
+  uint32_t NT = std::max(nt, b->step_nt), NG = std::max(ng, b->step_ng), NM = std::max(nm, b->step_nm);
+  StepLayout L = step_layout(NT, NG, NM);
+  if (b->dstep) cudaFree(b->dstep);
+  if (b->hstep) cudaFreeHost(b->hstep);
+  if (b->dprog) cudaFree(b->dprog);
+  b->dstep = b->hstep = nullptr;
+  b->dprog = nullptr;
+  CKB(cudaMalloc(&b->dstep, L.total));
+  CKB(cudaMallocHost(&b->hstep, L.total));
+  CKB(cudaMalloc(reinterpret_cast<void **>(&b->dprog),
+                 sizeof(Instr) * size_t(NT) * b->pcap + sizeof(Item) * NT + 256));
+  b->ditems = reinterpret_cast<Item *>(reinterpret_cast<char *>(b->dprog) + sizeof(Instr) * size_t(NT) * b->pcap);
+  b->step_nt = NT;
+  b->step_ng = NG;
+  b->step_nm = NM;
+  b->step_bytes = L.total;
+  return TN_OK;
+}
+
+int launch_step(tn_batch *b, uint32_t nt, const StepLayout &L, char *dbase) {
+  const int *list = reinterpret_cast<const int *>(dbase + L.list);
+  const int *order = reinterpret_cast<const int *>(dbase + L.order);
+  CKB(launch_compile(b->dtraj, list, int(nt), order, reinterpret_cast<const int *>(dbase + L.goff),
+                     reinterpret_cast<const int *>(dbase + L.gks), reinterpret_cast<const int *>(dbase + L.moff),
+                     reinterpret_cast<const int *>(dbase + L.mks), b->pcap, b->dprog, b->ditems, b->st));
+  CKB(cudaMemsetAsync(b->dcounter, 0, sizeof(int), b->st));
+  LaunchArgs la{};
+  la.items = b->ditems;
+  la.nitems = int(nt);
+  la.counter = b->dcounter;
+  la.trajs = b->dtraj;
+  la.prog = b->dprog;
+  la.gates = reinterpret_cast<const double *>(dbase + L.gates);
+  la.us = reinterpret_cast<const double *>(dbase + L.us);
+  la.outcomes = reinterpret_cast<int *>(dbase + L.outc);
+  la.probs = reinterpret_cast<double *>(dbase + L.probs);
+  la.ents = reinterpret_cast<double *>(dbase + L.ents);
+  la.pout = reinterpret_cast<double *>(dbase + L.probs);
+  la.ws = b->ws;
+  la.ws_stride = b->ws_stride;
+  la.max_sweeps = 40;
+  const int grid = std::min<int>(int(nt), b->grid_max);
+  CKB(launch_run(b->prec, la, grid, b->sortP, b->maxcap, b->st));
+  return TN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tn_batch_create(uint32_t ntraj, const uint32_t *ns, const tn_trunc *truncs, int32_t precision,
+                    const uint32_t *chi_caps, tn_batch **out) {
+  if (!out || !ns || ntraj == 0) return TN_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (precision != TN_PREC_F64 && precision != TN_PREC_MIXED) return TN_ERR_INVALID_ARG;
+  for (uint32_t i = 0; i < ntraj; ++i) {
+    if (ns[i] == 0) return TN_ERR_EMPTY_SYSTEM;
+    if (truncs && (truncs[i].mode < 0 || truncs[i].mode > 3)) return TN_ERR_INVALID_ARG;
+  }
+  int cnt = 0;
+  if (cudaGetDeviceCount(&cnt) != cudaSuccess || cnt == 0) return TN_ERR_NO_DEVICE;
+  tn_batch *b = new tn_batch();
+  b->prec = precision;
+  b->ntraj = ntraj;
+  b->n_alloc.assign(ns, ns + ntraj);
+  b->cap.resize(ntraj);
+  b->h.resize(ntraj);
+  b->slot_bytes.resize(ntraj);
+  const size_t eb = precision == TN_PREC_F64 ? 16 : 8;
+  std::vector<size_t> off(ntraj);
+  size_t total = 0;
+  for (uint32_t i = 0; i < ntraj; ++i) {
+    uint32_t c;
+    if (chi_caps && chi_caps[i])
+      c = std::min(chi_caps[i], max_rank(ns[i]));
+    else if (truncs && (truncs[i].mode == TN_TRUNC_CONST || truncs[i].mode == TN_TRUNC_BOTH))
+      c = std::min(std::max<uint32_t>(1, truncs[i].chi_max), max_rank(ns[i]));
+    else
+      c = std::min<uint32_t>(max_rank(ns[i]), 256);
+    b->cap[i] = c;
+    size_t bytes = align256(size_t(2) * c * c * eb * ns[i]) + align256(sizeof(double) * size_t(c) * (ns[i] + 1)) +
+                   align256(sizeof(int) * (ns[i] + 1));
+    off[i] = total;
+    b->slot_bytes[i] = bytes;
+    total += bytes;
+    b->maxcap = std::max<int>(b->maxcap, int(c));
+    b->maxn = std::max<int>(b->maxn, int(ns[i]));
+  }
+  auto bail = [&](int s) {
+    tn_batch_free(b);
+    return s;
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return bail(fail(e, "cudaStreamCreate"));
+  e = cudaMalloc(&b->arena, std::max<size_t>(total, 256));
+  if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(arena)"));
+  e = cudaMalloc(reinterpret_cast<void **>(&b->dtraj), sizeof(TrajDev) * ntraj + sizeof(int) * (ntraj + 2));
+  if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(traj)"));
+  b->dstatus = reinterpret_cast<int *>(b->dtraj + ntraj);
+  b->dcounter = b->dstatus + ntraj;
+  for (uint32_t i = 0; i < ntraj; ++i) {
+    TrajDev &d = b->h[i];
+    char *base = reinterpret_cast<char *>(b->arena) + off[i];
+    const uint32_t c = b->cap[i], n = ns[i];
+    d.gamma = base;
+    d.lam = reinterpret_cast<double *>(base + align256(size_t(2) * c * c * eb * n));
+    d.chi = reinterpret_cast<int *>(reinterpret_cast<char *>(d.lam) + align256(sizeof(double) * size_t(c) * (n + 1)));
+    d.status = b->dstatus + i;
+    d.n = int(n);
+    d.cap = int(c);
+    if (truncs) {
+      d.trunc_mode = truncs[i].mode;
+      d.chi_max = int(std::min<uint32_t>(truncs[i].chi_max, 0x7fffffff));
+      d.cutoff = truncs[i].cutoff;
+    } else {
+      d.trunc_mode = TN_TRUNC_NONE;
+      d.chi_max = 0;
+      d.cutoff = 0.0;
+    }
+  }
+  e = cudaMemcpyAsync(b->dtraj, b->h.data(), sizeof(TrajDev) * ntraj, cudaMemcpyHostToDevice, b->st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->dstatus, 0, sizeof(int) * (ntraj + 2), b->st);
+  if (e != cudaSuccess) return bail(fail(e, "init"));
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
+  b->sortP = next_pow2(2 * b->maxcap);
+  b->bps = run_blocks_per_sm(precision, b->sortP);
+  b->grid_max = std::max(1, b->sms * b->bps);
+  b->grid_max = std::min<int>(b->grid_max, int(ntraj));
+  b->ws_stride = run_work_bytes(precision, b->maxcap);
+  e = cudaMalloc(&b->ws, b->ws_stride * b->grid_max);
+  if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(workspace)"));
+  b->pcap = 4 * b->maxn + 8;
+  // reset all slots to |0...0>
+  std::vector<int> all(ntraj);
+  std::iota(all.begin(), all.end(), 0);
+  int *dlist = nullptr;
+  e = cudaMalloc(&dlist, sizeof(int) * ntraj);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dlist, all.data(), sizeof(int) * ntraj, cudaMemcpyHostToDevice, b->st);
+  if (e == cudaSuccess) e = launch_reset(b->dtraj, dlist, int(ntraj), precision, b->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+  if (dlist) cudaFree(dlist);
+  if (e != cudaSuccess) return bail(fail(e, "reset"));
+  *out = b;
+  return TN_OK;
+}
+
+int tn_batch_free(tn_batch *b) {
+  if (!b) return TN_OK;
+  if (b->st) cudaStreamSynchronize(b->st);
+  for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
+  if (b->din) cudaFree(b->din);
+  if (b->dprog) cudaFree(b->dprog);
+  if (b->dstep) cudaFree(b->dstep);
+  if (b->hstep) cudaFreeHost(b->hstep);
+  if (b->ws) cudaFree(b->ws);
+  if (b->dtraj) cudaFree(b->dtraj);
+  if (b->arena) cudaFree(b->arena);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+  return TN_OK;
+}
+
+int tn_batch_reset(tn_batch *b, uint32_t t, uint32_t n, const tn_trunc *trunc) {
+  if (!b || t >= b->ntraj) return TN_ERR_INVALID_ARG;
+  if (n == 0) return TN_ERR_EMPTY_SYSTEM;
+  if (n > b->n_alloc[t]) return TN_ERR_CAPACITY;
+  TrajDev &d = b->h[t];
+  uint32_t want = trunc && (trunc->mode == TN_TRUNC_CONST || trunc->mode == TN_TRUNC_BOTH)
+                      ? std::min(std::max<uint32_t>(1, trunc->chi_max), max_rank(n))
+                      : std::min<uint32_t>(max_rank(n), 256);
+  if (want > b->cap[t]) return TN_ERR_CAPACITY;
+  d.n = int(n);
+  if (trunc) {
+    d.trunc_mode = trunc->mode;
+    d.chi_max = int(std::min<uint32_t>(trunc->chi_max, 0x7fffffff));
+    d.cutoff = trunc->cutoff;
+  } else {
+    d.trunc_mode = TN_TRUNC_NONE;
+    d.chi_max = 0;
+    d.cutoff = 0.0;
+  }
+  CKB(cudaMemcpyAsync(b->dtraj + t, &d, sizeof(TrajDev), cudaMemcpyHostToDevice, b->st));
+  int *dl = b->dcounter + 1;
+  int tt = int(t);
+  CKB(cudaMemcpyAsync(dl, &tt, sizeof(int), cudaMemcpyHostToDevice, b->st));
+  CKB(launch_reset(b->dtraj, dl, 1, b->prec, b->st));
+  CKB(cudaStreamSynchronize(b->st));
+  return TN_OK;
+}
+
+int tn_batch_step(tn_batch *b, const uint32_t *trajs, uint32_t nt, const uint32_t *gate_off, const uint32_t *gate_ks,
+                  const double *gates, const uint32_t *meas_off, const uint32_t *meas_ks, const double *us,
+                  int32_t *outcomes, double *probs, double *entropy) {
+  if (!b || !trajs || !gate_off || !meas_off) return TN_ERR_INVALID_ARG;
+  if (nt == 0) return TN_OK;
+  const uint32_t ng = gate_off[nt], nm = meas_off[nt];
+  if ((ng && (!gate_ks || !gates)) || (nm && (!meas_ks || !us))) return TN_ERR_INVALID_ARG;
+  for (uint32_t i = 0; i < nt; ++i) {
+    if (trajs[i] >= b->ntraj) return TN_ERR_INVALID_ARG;
+    if (gate_off[i + 1] < gate_off[i] || meas_off[i + 1] < meas_off[i]) return TN_ERR_INVALID_ARG;
+    const uint32_t n = uint32_t(b->h[trajs[i]].n);
+    for (uint32_t j = meas_off[i]; j < meas_off[i + 1]; ++j) {
+      if (meas_ks[j] >= n) return TN_ERR_INVALID_ARG;
+      if (j > meas_off[i] && meas_ks[j] <= meas_ks[j - 1]) return TN_ERR_INVALID_ARG;
+    }
+  }
+  int need = 8;
+  for (uint32_t i = 0; i < nt; ++i)
+    need = std::max<int>(need, int(gate_off[i + 1] - gate_off[i]) + int(meas_off[i + 1] - meas_off[i]) +
+                                   2 * b->h[trajs[i]].n + 4);
+  if (need > b->pcap) {  // grow the per-trajectory program capacity
+    b->pcap = need;
+    b->step_nt = 0;
+  }
+  if (int s = ensure_step(b, nt, ng, nm)) return s;
+  StepLayout L = step_layout(b->step_nt, b->step_ng, b->step_nm);
+  char *hb = reinterpret_cast<char *>(b->hstep);
+  // most expensive first: cost ~ program length * chi^3
+  std::vector<std::pair<double, uint32_t>> cost(nt);
+  for (uint32_t i = 0; i < nt; ++i) {
+    const TrajDev &d = b->h[trajs[i]];
+    double c = std::min<double>(d.cap, double(max_rank(uint32_t(d.n))));
+    double ops = double(gate_off[i + 1] - gate_off[i]) + (meas_off[i + 1] > meas_off[i] ? 2.0 * d.n : 0.0) + 1.0;
+    cost[i] = {-(ops * c * c * c), i};
+  }
+  std::stable_sort(cost.begin(), cost.end());
+  int *ord = reinterpret_cast<int *>(hb + L.order);
+  for (uint32_t r = 0; r < nt; ++r) ord[cost[r].second] = int(r);
+  int *lst = reinterpret_cast<int *>(hb + L.list);
+  int *go = reinterpret_cast<int *>(hb + L.goff);
+  int *mo = reinterpret_cast<int *>(hb + L.moff);
+  for (uint32_t i = 0; i < nt; ++i) lst[i] = int(trajs[i]);
+  for (uint32_t i = 0; i <= nt; ++i) {
+    go[i] = int(gate_off[i]);
+    mo[i] = int(meas_off[i]);
+  }
+  int *gk = reinterpret_cast<int *>(hb + L.gks);
+  int *mk = reinterpret_cast<int *>(hb + L.mks);
+  for (uint32_t j = 0; j < ng; ++j) gk[j] = int(gate_ks[j]);
+  for (uint32_t j = 0; j < nm; ++j) mk[j] = int(meas_ks[j]);
+  if (ng) std::memcpy(hb + L.gates, gates, sizeof(double) * 32 * ng);
+  if (nm) std::memcpy(hb + L.us, us, sizeof(double) * nm);
+  CKB(cudaMemcpyAsync(b->dstep, b->hstep, L.in_bytes, cudaMemcpyHostToDevice, b->st));
+  if (int s = launch_step(b, nt, L, reinterpret_cast<char *>(b->dstep))) return s;
+  const size_t out_bytes = L.total - L.out_off;
+  CKB(cudaMemcpyAsync(hb + L.out_off, reinterpret_cast<char *>(b->dstep) + L.out_off, out_bytes,
+                      cudaMemcpyDeviceToHost, b->st));
+  CKB(cudaStreamSynchronize(b->st));
+  if (outcomes && nm) std::memcpy(outcomes, hb + L.outc, sizeof(int) * nm);
+  if (probs && nm) std::memcpy(probs, hb + L.probs, sizeof(double) * nm);
+  if (entropy) std::memcpy(entropy, hb + L.ents, sizeof(double) * nt);
+  return TN_OK;
+}
+
+int tn_batch_device_inputs(tn_batch *b, uint32_t max_gates, uint32_t max_meas, void **d_trajs, void **d_gate_off,
+                           void **d_gate_ks, void **d_gates, void **d_meas_off, void **d_meas_ks, void **d_us,
+                           void **d_outcomes, void **d_probs, void **d_entropy) {
+  if (!b) return TN_ERR_INVALID_ARG;
+  if (b->din) {
+    cudaFree(b->din);
+    b->din = nullptr;
+    for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    b->graphs.clear();
+  }
+  if (int s = ensure_step(b, b->ntraj, max_gates, max_meas)) return s;
+  StepLayout L = step_layout(b->ntraj, max_gates, max_meas);
+  CKB(cudaMalloc(&b->din, L.total));
+  b->din_gates = max_gates;
+  b->din_meas = max_meas;
+  char *d = reinterpret_cast<char *>(b->din);
+  // execution order = list order in this mode
+  std::vector<int> ident(b->ntraj);
+  std::iota(ident.begin(), ident.end(), 0);
+  CKB(cudaMemcpy(d + L.order, ident.data(), sizeof(int) * b->ntraj, cudaMemcpyHostToDevice));
+  if (d_trajs) *d_trajs = d + L.list;
+  if (d_gate_off) *d_gate_off = d + L.goff;
+  if (d_gate_ks) *d_gate_ks = d + L.gks;
+  if (d_gates) *d_gates = d + L.gates;
+  if (d_meas_off) *d_meas_off = d + L.moff;
+  if (d_meas_ks) *d_meas_ks = d + L.mks;
+  if (d_us) *d_us = d + L.us;
+  if (d_outcomes) *d_outcomes = d + L.outc;
+  if (d_probs) *d_probs = d + L.probs;
+  if (d_entropy) *d_entropy = d + L.ents;
+  return TN_OK;
+}
+
+int tn_batch_step_device(tn_batch *b, uint32_t nt) {
+  if (!b || !b->din || nt > b->ntraj) return TN_ERR_INVALID_ARG;
+  if (nt == 0) return TN_OK;
+  StepLayout L = step_layout(b->ntraj, b->din_gates, b->din_meas);
+  auto it = b->graphs.find(nt);
+  if (it == b->graphs.end()) {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    CKB(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+    int s = launch_step(b, nt, L, reinterpret_cast<char *>(b->din));
+    cudaError_t e = cudaStreamEndCapture(b->st, &g);
+    if (s != TN_OK) {
+      if (g) cudaGraphDestroy(g);
+      return s;
+    }
+    if (e != cudaSuccess) return fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(e, "cudaGraphInstantiate");
+    it = b->graphs.emplace(nt, ge).first;
+  }
+  CKB(cudaGraphLaunch(it->second, b->st));
+  return TN_OK;
+}
+
+int tn_batch_synchronize(tn_batch *b) {
+  if (!b) return TN_ERR_INVALID_ARG;
+  CKB(cudaStreamSynchronize(b->st));
+  return TN_OK;
+}
+
+int tn_batch_bond_dims(tn_batch *b, uint32_t t, uint32_t *out, uint32_t cap) {
+  if (!b || t >= b->ntraj || !out) return TN_ERR_INVALID_ARG;
+  const TrajDev &d = b->h[t];
+  if (d.n < 2) return TN_NONE;
+  if (cap < uint32_t(d.n - 1)) return TN_ERR_INVALID_ARG;
+  std::vector<int> chi(d.n + 1);
+  CKB(cudaMemcpyAsync(chi.data(), d.chi, sizeof(int) * (d.n + 1), cudaMemcpyDeviceToHost, b->st));
+  CKB(cudaStreamSynchronize(b->st));
+  for (int i = 0; i < d.n - 1; ++i) out[i] = uint32_t(chi[i + 1]);
+  return TN_OK;
+}
+
+int tn_batch_svals(tn_batch *b, uint32_t t, uint32_t bond, double *out, uint32_t cap, uint32_t *len) {
+  if (!b || t >= b->ntraj) return TN_ERR_INVALID_ARG;
+  const TrajDev &d = b->h[t];
+  if (d.n < 2 || bond >= uint32_t(d.n - 1)) return TN_NONE;
+  int l = 0;
+  CKB(cudaMemcpyAsync(&l, d.chi + bond + 1, sizeof(int), cudaMemcpyDeviceToHost, b->st));
+  CKB(cudaStreamSynchronize(b->st));
+  if (len) *len = uint32_t(l);
+  if (!out) return TN_OK;
+  if (cap < uint32_t(l)) return TN_ERR_INVALID_ARG;
+  CKB(cudaMemcpyAsync(out, d.lam + size_t(bond + 1) * d.cap, sizeof(double) * l, cudaMemcpyDeviceToHost, b->st));
+  CKB(cudaStreamSynchronize(b->st));
+  return TN_OK;
+}
+
+int tn_batch_device_status(tn_batch *b, int32_t *status) {
+  if (!b || !status) return TN_ERR_INVALID_ARG;
+  std::vector<int> v(b->ntraj);
+  CKB(cudaMemcpyAsync(v.data(), b->dstatus, sizeof(int) * b->ntraj, cudaMemcpyDeviceToHost, b->st));
+  CKB(cudaMemsetAsync(b->dstatus, 0, sizeof(int) * b->ntraj, b->st));
+  CKB(cudaStreamSynchronize(b->st));
+  int acc = 0;
+  for (int x : v) acc |= x;
+  *status = acc;
+  return TN_OK;
+}
+
+int tn_batch_slot_bytes(tn_batch *b, uint32_t t, uint64_t *bytes) {
+  if (!b || t >= b->ntraj || !bytes) return TN_ERR_INVALID_ARG;
+  *bytes = b->slot_bytes[t];
+  return TN_OK;
+}
+
+int tn_batch_stream(tn_batch *b, void **stream) {
+  if (!b || !stream) return TN_ERR_INVALID_ARG;
+  *stream = reinterpret_cast<void *>(b->st);
+  return TN_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,915 @@
+// tn_device.cuh -- device side of the Gamma-Lambda MPS trajectory engine (sm_103a).
+//
+// One CTA owns one trajectory for the whole of a launch and executes that
+// trajectory's instruction list (gates, refactors, measurements, entropy reads)
+// in order.  Trajectory state stays in HBM between launches:
+//   gamma : n slots of 2*cap*cap complex<T>; site k holds Gamma_k as a dense
+//           row-major (chi_{k-1}, 2, chi_k) array at the slot start (the
+//           reference layout, tensor-net/lib/mps.rs:344-349);
+//   lam   : n+1 slots of cap float64; slot 0 and slot n hold [1.0] so that the
+//           chain-end branches of the reference collapse into one formula,
+//           slot b+1 holds Lambda_b (mps.rs:352-353);
+//   chi   : n+1 ints, chi[b+1] = dim of bond b, chi[0] = chi[n] = 1.
+// A bond operation on (k, k+1) follows local_refactor / apply_unitary2
+// (mps.rs:846-880, 1332-1387): theta build -> one-sided Jacobi SVD -> sort,
+// truncate, renormalise (process_svd, mps.rs:236-293) -> Gamma rebuild and
+// local_renormalize (mps.rs:1147-1209).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "tn_internal.h"
+
+namespace tn {
+
+// ---------------------------------------------------------------- complex
+template <typename T>
+struct __align__(2 * sizeof(T)) cpx {
+  T x, y;
+};
+
+template <typename T>
+__device__ __forceinline__ cpx<T> mkc(T x, T y) {
+  cpx<T> r;
+  r.x = x;
+  r.y = y;
+  return r;
+}
+template <typename T>
+__device__ __forceinline__ cpx<T> czero() {
+  return mkc<T>(T(0), T(0));
+}
+template <typename T>
+__device__ __forceinline__ cpx<T> cadd(cpx<T> a, cpx<T> b) {
+  return mkc<T>(a.x + b.x, a.y + b.y);
+}
+template <typename T>
+__device__ __forceinline__ cpx<T> cmul(cpx<T> a, cpx<T> b) {
+  return mkc<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename T>
+__device__ __forceinline__ cpx<T> cscale(cpx<T> a, T s) {
+  return mkc<T>(a.x * s, a.y * s);
+}
+// acc + a*b
+template <typename T>
+__device__ __forceinline__ cpx<T> cfma(cpx<T> a, cpx<T> b, cpx<T> acc) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+  return acc;
+}
+// acc + conj(a)*b
+template <typename T>
+__device__ __forceinline__ cpx<T> cjfma(cpx<T> a, cpx<T> b, cpx<T> acc) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(-a.y, b.x, acc.y);
+  return acc;
+}
+template <typename T>
+__device__ __forceinline__ T cabs2(cpx<T> a) {
+  return a.x * a.x + a.y * a.y;
+}
+
+template <typename T>
+struct Eps;
+template <>
+struct Eps<double> {
+  static constexpr double v = 2.220446049250313e-16;
+};
+template <>
+struct Eps<float> {
+  static constexpr float v = 1.1920929e-07f;
+};
+
+// --------------------------------------------------------- block helpers
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double *red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    double t = (lane < NT / 32) ? red[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) red[32] = t;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+template <int NT>
+__device__ __forceinline__ void block_sum2(double &a, double &b, double *red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  __syncthreads();
+  if (lane == 0) {
+    red[warp] = a;
+    red[32 + warp] = b;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    double t = (lane < NT / 32) ? red[lane] : 0.0;
+    double u = (lane < NT / 32) ? red[32 + lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      t += __shfl_xor_sync(0xffffffffu, t, o);
+      u += __shfl_xor_sync(0xffffffffu, u, o);
+    }
+    if (lane == 0) {
+      red[64] = t;
+      red[65] = u;
+    }
+  }
+  __syncthreads();
+  a = red[64];
+  b = red[65];
+}
+
+template <int NT>
+__device__ __forceinline__ int block_min_int(int v, int *red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    int t = (lane < NT / 32) ? red[lane] : 0x7fffffff;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t = min(t, __shfl_xor_sync(0xffffffffu, t, o));
+    if (lane == 0) red[32] = t;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+// ------------------------------------------------------- shared layout
+// W = columns per Jacobi block pair (two blocks of W/2).  TU = inner-dim
+// chunk of the theta build.
+template <typename T, int W>
+struct SmemLayout {
+  static constexpr int TU = 16;
+  static constexpr int TILE = 32;                 // theta tile: 32 (v) x 32 (w)
+  static constexpr int TP = W + 1;                // padded row pitch of Ts
+  // region 0: theta tiles or sort keys (double) + perm (int)
+  static constexpr size_t gemm_bytes = size_t(2) * TILE * 2 * TU * sizeof(cpx<T>);
+  __host__ __device__ static size_t sort_bytes(int P) { return size_t(P) * (sizeof(double) + sizeof(int)); }
+  __host__ __device__ static size_t region0(int P) {
+    size_t g = gemm_bytes, s = sort_bytes(P);
+    size_t r = g > s ? g : s;
+    return (r + 255) & ~size_t(255);
+  }
+  static constexpr size_t g_bytes = size_t(W) * W * sizeof(cpx<T>);
+  static constexpr size_t ts_bytes = size_t(32) * TP * sizeof(cpx<T>);
+  static constexpr size_t rot_bytes = size_t(W / 2) * (2 * sizeof(T) + sizeof(cpx<T>) + sizeof(int)) + 64;
+  static constexpr size_t red_bytes = 128 * sizeof(double);
+  __host__ __device__ static size_t total(int P) {
+    return region0(P) + 2 * g_bytes + ts_bytes + rot_bytes + red_bytes + 128 * sizeof(int) + 256;
+  }
+};
+
+template <typename T, int W>
+struct Smem {
+  unsigned char *r0;
+  cpx<T> *G, *J, *Ts;
+  T *rc, *rs;
+  cpx<T> *re;
+  int *rflag;
+  double *red;
+  int *ired;
+  __device__ Smem(unsigned char *base, int P) {
+    using L = SmemLayout<T, W>;
+    unsigned char *p = base;
+    r0 = p;
+    p += L::region0(P);
+    G = reinterpret_cast<cpx<T> *>(p);
+    p += L::g_bytes;
+    J = reinterpret_cast<cpx<T> *>(p);
+    p += L::g_bytes;
+    Ts = reinterpret_cast<cpx<T> *>(p);
+    p += L::ts_bytes;
+    re = reinterpret_cast<cpx<T> *>(p);
+    p += (W / 2) * sizeof(cpx<T>);
+    rc = reinterpret_cast<T *>(p);
+    p += (W / 2) * sizeof(T);
+    rs = reinterpret_cast<T *>(p);
+    p += (W / 2) * sizeof(T);
+    rflag = reinterpret_cast<int *>(p);
+    p += (W / 2) * sizeof(int) + 64 - ((W / 2) * sizeof(int)) % 64;
+    p = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15));
+    red = reinterpret_cast<double *>(p);
+    p += 128 * sizeof(double);
+    ired = reinterpret_cast<int *>(p);
+  }
+};
+
+// ------------------------------------------------------------- workspace
+template <typename T>
+struct Work {
+  cpx<T> *A;     // Jacobi vectors, vector-contiguous, up to 4*cap^2
+  cpx<T> *V;     // accumulated rotations, up to 4*cap^2
+  T *scl;        // 2*cap row/column scale factors
+  double *s2;    // 2*cap kept Schmidt values
+  int *perm;     // 2*cap
+};
+
+template <typename T>
+__host__ __device__ inline size_t work_bytes(int cap) {
+  size_t n4 = size_t(4) * cap * cap;
+  size_t b = 2 * n4 * sizeof(cpx<T>) + size_t(2) * cap * sizeof(T) + size_t(2) * cap * sizeof(double) +
+             size_t(2) * cap * sizeof(int);
+  return (b + 255) & ~size_t(255);
+}
+
+template <typename T>
+__device__ inline Work<T> make_work(void *base, int cap) {
+  Work<T> w;
+  unsigned char *p = reinterpret_cast<unsigned char *>(base);
+  size_t n4 = size_t(4) * cap * cap;
+  w.A = reinterpret_cast<cpx<T> *>(p);
+  p += n4 * sizeof(cpx<T>);
+  w.V = reinterpret_cast<cpx<T> *>(p);
+  p += n4 * sizeof(cpx<T>);
+  w.s2 = reinterpret_cast<double *>(p);
+  p += size_t(2) * cap * sizeof(double);
+  w.scl = reinterpret_cast<T *>(p);
+  p += size_t(2) * cap * sizeof(T);
+  w.perm = reinterpret_cast<int *>(p);
+  return w;
+}
+
+__device__ __forceinline__ bool is_normal_pos(double s, double eps) {
+  // f64::is_normal() && s > eps  (mps.rs:254-258, 262-266)
+  return isfinite(s) && s != 0.0 && fabs(s) >= 2.2250738585072014e-308 && s > eps;
+}
+
+// Round-robin (circle method) pairing: round r of W-1, pair t of W/2.
+template <int W>
+__device__ __forceinline__ void rr_pair(int r, int t, int &p, int &q) {
+  auto pos = [&](int x) { return x == 0 ? 0 : ((x - 1 + r) % (W - 1)) + 1; };
+  int a = pos(t), b = pos(W - 1 - t);
+  p = a < b ? a : b;
+  q = a < b ? b : a;
+}
+
+// =======================================================================
+// Phase 1: theta = Lambda_{k-1} Gamma_k Lambda_k Gamma_{k+1} Lambda_{k+1},
+// then op on the fused physical pair (do_contract2 mps.rs:628-651,
+// contract_local2 732-754, apply_unitary2 1343-1352).
+// Writes A vector-contiguous: colmode A[j*m + i] = theta[i][j] (vectors =
+// columns, m >= nc), else A[i*nc + j] = theta[i][j] (vectors = rows).
+// =======================================================================
+template <typename T, int NT, int W>
+__device__ void build_theta(const cpx<T> *__restrict__ gk, const cpx<T> *__restrict__ gk1,
+                            const double *__restrict__ lamL, const double *__restrict__ lamM,
+                            const double *__restrict__ lamR, int cL, int cM, int cR,
+                            const double *__restrict__ gate, cpx<T> *__restrict__ A, bool colmode,
+                            Smem<T, W> &sm) {
+  using L = SmemLayout<T, W>;
+  constexpr int TILE = L::TILE, TU = L::TU;
+  constexpr int PER = (TILE * TILE) / NT;  // (v,w) outputs per thread
+  static_assert(PER >= 1 && (TILE * TILE) % NT == 0, "tile/threads");
+  cpx<T> *Xs = reinterpret_cast<cpx<T> *>(sm.r0);  // [TILE v][2][TU]
+  cpx<T> *Ys = Xs + TILE * 2 * TU;                // [TU][2][TILE w]
+  const int m = 2 * cL, nc = 2 * cR;
+  const int ell = colmode ? m : nc;
+
+  cpx<T> op[16];
+  if (gate) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) op[i] = mkc<T>(T(gate[2 * i]), T(gate[2 * i + 1]));
+  }
+  const int tid = threadIdx.x;
+  for (int v0 = 0; v0 < cL; v0 += TILE) {
+    for (int w0 = 0; w0 < cR; w0 += TILE) {
+      cpx<T> acc[PER][4];
+#pragma unroll
+      for (int e = 0; e < PER; ++e)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[e][q] = czero<T>();
+      for (int u0 = 0; u0 < cM; u0 += TU) {
+        __syncthreads();
+        for (int idx = tid; idx < TILE * 2 * TU; idx += NT) {
+          int u = idx % TU, s = (idx / TU) & 1, v = idx / (2 * TU);
+          int gv = v0 + v, gu = u0 + u;
+          cpx<T> x = czero<T>();
+          if (gv < cL && gu < cM) x = gk[(size_t(gv) * 2 + s) * cM + gu];
+          Xs[idx] = x;
+        }
+        for (int idx = tid; idx < TU * 2 * TILE; idx += NT) {
+          int w = idx % TILE, s = (idx / TILE) & 1, u = idx / (2 * TILE);
+          int gw = w0 + w, gu = u0 + u;
+          cpx<T> y = czero<T>();
+          if (gw < cR && gu < cM) y = cscale(gk1[(size_t(gu) * 2 + s) * cR + gw], T(lamM[gu]));
+          Ys[idx] = y;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < PER; ++e) {
+          int o = tid + e * NT;
+          int v = o / TILE, w = o % TILE;
+#pragma unroll 4
+          for (int u = 0; u < TU; ++u) {
+            cpx<T> x0 = Xs[(v * 2 + 0) * TU + u], x1 = Xs[(v * 2 + 1) * TU + u];
+            cpx<T> y0 = Ys[(u * 2 + 0) * TILE + w], y1 = Ys[(u * 2 + 1) * TILE + w];
+            acc[e][0] = cfma(x0, y0, acc[e][0]);
+            acc[e][1] = cfma(x0, y1, acc[e][1]);
+            acc[e][2] = cfma(x1, y0, acc[e][2]);
+            acc[e][3] = cfma(x1, y1, acc[e][3]);
+          }
+        }
+      }
+      // epilogue: Lambda_{k-1}, Lambda_{k+1} scaling, gate on (s1 s2), store
+#pragma unroll
+      for (int e = 0; e < PER; ++e) {
+        int o = tid + e * NT;
+        int v = v0 + o / TILE, w = w0 + o % TILE;
+        if (v < cL && w < cR) {
+          T sl = T(lamL[v]), sr = T(lamR[w]);
+          cpx<T> th[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) th[q] = cscale(cscale(acc[e][q], sl), sr);
+          if (gate) {
+            cpx<T> t2[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+              cpx<T> s = czero<T>();
+#pragma unroll
+              for (int b = 0; b < 4; ++b) s = cfma(op[a * 4 + b], th[b], s);
+              t2[a] = s;
+            }
+#pragma unroll
+            for (int a = 0; a < 4; ++a) th[a] = t2[a];
+          }
+#pragma unroll
+          for (int a = 0; a < 4; ++a) {
+            int s1 = a >> 1, s2 = a & 1;
+            int i = 2 * v + s1, j = s2 * cR + w;
+            if (colmode)
+              A[size_t(j) * ell + i] = th[a];
+            else
+              A[size_t(i) * ell + j] = th[a];
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// =======================================================================
+// Phase 2: one-sided (Hestenes) block Jacobi on the c vectors of length ell
+// stored in A; V (c x c, vector-contiguous) accumulates the right rotation.
+// Block pairs of W vectors: Gram G = Ab^H Ab (W x W), one cyclic sweep of
+// two-sided Jacobi on G with parallel (round-robin) ordering accumulating J,
+// then Ab <- Ab J and Vb <- Vb J.  Converged when every pair satisfies
+// |a_p^H a_q| <= tol * |a_p| |a_q| with tol = sqrt(ell) * eps.
+// Returns the number of outer sweeps, or -1 if the sweep limit was hit.
+// =======================================================================
+template <typename T, int NT, int W>
+__device__ void load_block_chunk(const cpx<T> *__restrict__ A, int ell, const int *cols, int wcnt, int i0,
+                                 cpx<T> *Ts) {
+  constexpr int TP = W + 1;
+  for (int idx = threadIdx.x; idx < 32 * W; idx += NT) {
+    int r = idx & 31, p = idx >> 5;
+    cpx<T> v = czero<T>();
+    if (p < wcnt && i0 + r < ell) v = A[size_t(cols[p]) * ell + i0 + r];
+    Ts[r * TP + p] = v;
+  }
+}
+
+template <typename T, int NT, int W>
+__device__ void gram_block(const cpx<T> *__restrict__ A, int ell, const int *cols, int wcnt, Smem<T, W> &sm) {
+  constexpr int TP = W + 1;
+  constexpr int PER = (W * W + NT - 1) / NT;
+  cpx<T> acc[PER];
+#pragma unroll
+  for (int e = 0; e < PER; ++e) acc[e] = czero<T>();
+  for (int i0 = 0; i0 < ell; i0 += 32) {
+    __syncthreads();
+    load_block_chunk<T, NT, W>(A, ell, cols, wcnt, i0, sm.Ts);
+    __syncthreads();
+    const int rmax = min(32, ell - i0);
+#pragma unroll
+    for (int e = 0; e < PER; ++e) {
+      int o = threadIdx.x + e * NT;
+      if (o < W * W) {
+        int p = o / W, q = o % W;
+        cpx<T> a = acc[e];
+        for (int r = 0; r < rmax; ++r) a = cjfma(sm.Ts[r * TP + p], sm.Ts[r * TP + q], a);
+        acc[e] = a;
+      }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < PER; ++e) {
+    int o = threadIdx.x + e * NT;
+    if (o < W * W) sm.G[o] = acc[e];
+  }
+  __syncthreads();
+}
+
+// X (rows x W slice of a vector-contiguous matrix with vector length ld) <- X J
+template <typename T, int NT, int W>
+__device__ void apply_right_block(cpx<T> *__restrict__ X, int ld, int rows, const int *cols, int wcnt,
+                                  Smem<T, W> &sm) {
+  constexpr int TP = W + 1;
+  constexpr int PER = (32 * W + NT - 1) / NT;
+  for (int i0 = 0; i0 < rows; i0 += 32) {
+    __syncthreads();
+    load_block_chunk<T, NT, W>(X, ld, cols, wcnt, i0, sm.Ts);
+    __syncthreads();
+    cpx<T> out[PER];
+#pragma unroll
+    for (int e = 0; e < PER; ++e) {
+      int o = threadIdx.x + e * NT;
+      out[e] = czero<T>();
+      if (o < 32 * W) {
+        int q = o >> 5, r = o & 31;
+        if (q < wcnt) {
+          cpx<T> a = czero<T>();
+          for (int p = 0; p < wcnt; ++p) a = cfma(sm.Ts[r * TP + p], sm.J[p * W + q], a);
+          out[e] = a;
+        }
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < PER; ++e) {
+      int o = threadIdx.x + e * NT;
+      if (o < 32 * W) {
+        int q = o >> 5, r = o & 31;
+        if (q < wcnt && i0 + r < rows) X[size_t(cols[q]) * ld + i0 + r] = out[e];
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// Diagonalise the Hermitian W x W Gram matrix in sm.G by `nsweep` cyclic
+// sweeps with round-robin ordering; J accumulates the rotations (starts at I).
+template <typename T, int NT, int W>
+__device__ void jacobi_gram(Smem<T, W> &sm, int wcnt, T tol, int nsweep) {
+  constexpr int H = W / 2;
+  for (int idx = threadIdx.x; idx < W * W; idx += NT) {
+    int p = idx / W, q = idx % W;
+    sm.J[idx] = (p == q) ? mkc<T>(T(1), T(0)) : czero<T>();
+  }
+  __syncthreads();
+  for (int sw = 0; sw < nsweep; ++sw) {
+    for (int r = 0; r < W - 1; ++r) {
+      if (threadIdx.x < H) {
+        int t = threadIdx.x, p, q;
+        rr_pair<W>(r, t, p, q);
+        int flag = 0;
+        T c = T(1), s = T(0);
+        cpx<T> e = mkc<T>(T(1), T(0));
+        if (q < wcnt) {
+          T a = sm.G[p * W + p].x, b = sm.G[q * W + q].x;
+          cpx<T> g = sm.G[p * W + q];
+          T ag = sqrt(cabs2(g));
+          if (a > T(0) && b > T(0) && ag > tol * sqrt(a) * sqrt(b)) {
+            T zeta = (b - a) / (T(2) * ag);
+            T t_ = T(1) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+            if (zeta < T(0)) t_ = -t_;
+            c = T(1) / sqrt(T(1) + t_ * t_);
+            s = t_ * c;
+            e = mkc<T>(g.x / ag, -g.y / ag);  // e^{-i phi}, g = |g| e^{i phi}
+            flag = 1;
+          }
+        }
+        sm.rc[t] = c;
+        sm.rs[t] = s;
+        sm.re[t] = e;
+        sm.rflag[t] = flag;
+      }
+      __syncthreads();
+      // rows: G[p][j] <- c G[p][j] - s conj(e) G[q][j];  G[q][j] <- s G[p][j] + c conj(e) G[q][j]
+      for (int idx = threadIdx.x; idx < H * W; idx += NT) {
+        int t = idx / W, j = idx % W;
+        if (!sm.rflag[t]) continue;
+        int p, q;
+        rr_pair<W>(r, t, p, q);
+        T c = sm.rc[t], s = sm.rs[t];
+        cpx<T> ec = mkc<T>(sm.re[t].x, -sm.re[t].y);
+        cpx<T> gp = sm.G[p * W + j], gq = sm.G[q * W + j];
+        cpx<T> eq = cmul(ec, gq);
+        sm.G[p * W + j] = mkc<T>(c * gp.x - s * eq.x, c * gp.y - s * eq.y);
+        sm.G[q * W + j] = mkc<T>(s * gp.x + c * eq.x, s * gp.y + c * eq.y);
+      }
+      __syncthreads();
+      // columns of G and J: X[j][p] <- c X[j][p] - s e X[j][q];  X[j][q] <- s X[j][p] + c e X[j][q]
+      for (int idx = threadIdx.x; idx < 2 * H * W; idx += NT) {
+        int which = idx / (H * W);
+        int rem = idx % (H * W);
+        int t = rem / W, j = rem % W;
+        if (!sm.rflag[t]) continue;
+        int p, q;
+        rr_pair<W>(r, t, p, q);
+        T c = sm.rc[t], s = sm.rs[t];
+        cpx<T> e = sm.re[t];
+        cpx<T> *X = which ? sm.J : sm.G;
+        cpx<T> xp = X[j * W + p], xq = X[j * W + q];
+        cpx<T> eq = cmul(e, xq);
+        X[j * W + p] = mkc<T>(c * xp.x - s * eq.x, c * xp.y - s * eq.y);
+        X[j * W + q] = mkc<T>(s * xp.x + c * eq.x, s * xp.y + c * eq.y);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+template <typename T, int NT, int W>
+__device__ int jacobi_svd(cpx<T> *__restrict__ A, cpx<T> *__restrict__ V, int ell, int c, int max_sweeps,
+                          Smem<T, W> &sm) {
+  constexpr int B = W / 2;
+  const T tol = sqrt(T(ell)) * Eps<T>::v;
+  // V = I
+  for (size_t idx = threadIdx.x; idx < size_t(c) * c; idx += NT) {
+    int j = int(idx / c), i = int(idx % c);
+    V[idx] = (i == j) ? mkc<T>(T(1), T(0)) : czero<T>();
+  }
+  __syncthreads();
+  const int nblk = (c + B - 1) / B;
+  int *cols = sm.ired + 64;  // W ints (ired[0..64) is reduction scratch)
+  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    int rotated = 0;
+    const int npairs = (nblk <= 2) ? 1 : nblk * (nblk - 1) / 2;
+    int I = 0, Jb = 1;
+    for (int pr = 0; pr < npairs; ++pr) {
+      int wcnt, wi = 0, wj = 0;
+      if (nblk <= 2) {
+        wcnt = c;
+      } else {
+        wi = min(B, c - I * B);
+        wj = min(B, c - Jb * B);
+        wcnt = wi + wj;
+      }
+      if (threadIdx.x < W) {
+        const int t = threadIdx.x;
+        int col = 0;
+        if (nblk <= 2)
+          col = t < c ? t : 0;
+        else
+          col = (t < wi) ? I * B + t : ((t - wi) < wj ? Jb * B + (t - wi) : 0);
+        cols[t] = col;
+      }
+      __syncthreads();
+      gram_block<T, NT, W>(A, ell, cols, wcnt, sm);
+      // off-diagonal test
+      int need = 0;
+      for (int idx = threadIdx.x; idx < W * W; idx += NT) {
+        int p = idx / W, q = idx % W;
+        if (p < q && q < wcnt) {
+          T a = sm.G[p * W + p].x, b = sm.G[q * W + q].x;
+          T ag = sqrt(cabs2(sm.G[idx]));
+          if (a > T(0) && b > T(0) && ag > tol * sqrt(a) * sqrt(b)) need = 1;
+        }
+      }
+      need = __syncthreads_or(need);
+      if (need) {
+        rotated = 1;
+        jacobi_gram<T, NT, W>(sm, wcnt, tol, 1);
+        apply_right_block<T, NT, W>(A, ell, ell, cols, wcnt, sm);
+        apply_right_block<T, NT, W>(V, c, c, cols, wcnt, sm);
+      }
+      // next block pair (row-cyclic)
+      if (++Jb >= nblk) {
+        ++I;
+        Jb = I + 1;
+      }
+    }
+    if (!rotated) return sweep + 1;
+  }
+  return -1;
+}
+
+// =======================================================================
+// Phase 3: singular values, sort, process_svd (mps.rs:236-293), Gamma
+// rebuild (mps.rs:856-877 / 1357-1382), local_renormalize (1206-1209).
+// =======================================================================
+template <typename T, int NT, int W>
+__device__ void bitonic_desc(double *key, int *idx, int P) {
+  // order: key descending, index ascending on ties
+  for (int k = 2; k <= P; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int t = threadIdx.x; t < P; t += NT) {
+        int l = t ^ j;
+        if (l > t) {
+          bool up = ((t & k) == 0);
+          double ka = key[t], kb = key[l];
+          int ia = idx[t], ib = idx[l];
+          bool a_first = (ka > kb) || (ka == kb && ia < ib);
+          bool swap = up ? !a_first : a_first;
+          if (swap) {
+            key[t] = kb;
+            key[l] = ka;
+            idx[t] = ib;
+            idx[l] = ia;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+template <typename T, int NT, int W>
+__device__ void finalize_bond(const TrajDev &tr, int k, cpx<T> *__restrict__ gk, cpx<T> *__restrict__ gk1,
+                              const double *__restrict__ lamL, double *__restrict__ lamM,
+                              const double *__restrict__ lamR, int cL, int cR, bool colmode, int ell, int c,
+                              Work<T> &wk, Smem<T, W> &sm) {
+  const int P = [&] {
+    int p = 1;
+    while (p < c) p <<= 1;
+    return p;
+  }();
+  double *key = reinterpret_cast<double *>(sm.r0);
+  int *pidx = reinterpret_cast<int *>(key + P);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // column norms (float64 accumulation)
+  for (int j = warp; j < P; j += NT / 32) {
+    double acc = 0.0;
+    if (j < c) {
+      const cpx<T> *a = wk.A + size_t(j) * ell;
+      for (int i = lane; i < ell; i += 32) {
+        cpx<T> x = a[i];
+        acc += double(x.x) * double(x.x) + double(x.y) * double(x.y);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
+      key[j] = (j < c) ? sqrt(acc) : -1.0;
+      pidx[j] = j;
+    }
+  }
+  __syncthreads();
+  bitonic_desc<T, NT, W>(key, pidx, P);
+  // norm of all singular values, normalise
+  double part = 0.0;
+  for (int j = threadIdx.x; j < c; j += NT) part += key[j] * key[j];
+  const double norm1 = sqrt(block_sum<NT>(part, sm.red));
+  // rank rule on s/||s||
+  int mode = tr.trunc_mode;
+  double eps = (mode == 2 || mode == 3) ? fabs(tr.cutoff) : 2.220446049250313e-16;
+  // float32 theta carries ~sqrt(ell)*eps32 relative rounding: exact zeros of
+  // the spectrum come out at that level, so the MIXED path never keeps values
+  // below it (the float64 path keeps the reference's threshold unchanged).
+  if (sizeof(T) == 4) eps = fmax(eps, 2.0 * sqrt(double(ell)) * 1.1920928955078125e-07);
+  int firstbad = c;
+  for (int j = threadIdx.x; j < c; j += NT) {
+    double s = key[j] / norm1;
+    if (!is_normal_pos(s, eps)) firstbad = min(firstbad, j);
+  }
+  int nlead = block_min_int<NT>(firstbad, sm.ired);
+  int rank;
+  if (mode == 1) {
+    rank = min(max(tr.chi_max, 1), nlead);
+    if (rank < 1) rank = 1;  // all-zero spectrum: keep one vector instead of none
+  } else if (mode == 3) {
+    rank = max(1, min(tr.chi_max, nlead));
+  } else {
+    rank = max(nlead, 1);
+  }
+  if (rank > tr.cap) {
+    if (threadIdx.x == 0) atomicOr(tr.status, ST_CAPACITY);
+    rank = tr.cap;
+  }
+  double part2 = 0.0;
+  for (int j = threadIdx.x; j < rank; j += NT) {
+    double s = key[j] / norm1;
+    part2 += s * s;
+  }
+  const double norm2 = sqrt(block_sum<NT>(part2, sm.red));
+  // kept values s2 = (s/norm1)/norm2; scale factors for the rebuild
+  for (int j = threadIdx.x; j < rank; j += NT) {
+    double s1 = key[j] / norm1;
+    wk.s2[j] = s1 / norm2;
+    wk.perm[j] = pidx[j];
+  }
+  // scl[0..cL): 1/Lambda_{k-1}[v]; scl[cap..cap+cR): norm2/Lambda_{k+1}[w]
+  T *sclL = wk.scl, *sclR = wk.scl + tr.cap;
+  for (int v = threadIdx.x; v < cL; v += NT) sclL[v] = T(1.0 / lamL[v]);
+  for (int w = threadIdx.x; w < cR; w += NT) sclR[w] = T(norm2 / lamR[w]);
+  __syncthreads();
+  const int m = 2 * cL, nc = 2 * cR;
+  // Gamma_k[v,s1,j] = U[(v s1), j] / Lambda_{k-1}[v]
+  for (size_t idx = threadIdx.x; idx < size_t(m) * rank; idx += NT) {
+    int i = int(idx / rank), j = int(idx % rank);
+    int src = wk.perm[j];
+    cpx<T> u;
+    if (colmode) {
+      T inv = T(1.0 / key[j]);  // U[:, j] = A_src / sigma_src
+      u = cscale(wk.A[size_t(src) * ell + i], inv);
+    } else {
+      cpx<T> vv = wk.V[size_t(src) * c + i];
+      u = mkc<T>(vv.x, -vv.y);
+    }
+    gk[idx] = cscale(u, sclL[i >> 1]);
+  }
+  // Gamma_{k+1}[j, s2, w] = Vh[j, (s2 w)] * norm2 / Lambda_{k+1}[w]
+  for (size_t idx = threadIdx.x; idx < size_t(rank) * nc; idx += NT) {
+    int j = int(idx / nc), col = int(idx % nc);
+    int src = wk.perm[j];
+    cpx<T> vh;
+    if (colmode) {
+      cpx<T> vv = wk.V[size_t(src) * c + col];
+      vh = mkc<T>(vv.x, -vv.y);
+    } else {
+      T inv = T(1.0 / key[j]);  // Vh[j, :] = A_src / sigma_src
+      vh = cscale(wk.A[size_t(src) * ell + col], inv);
+    }
+    int w = col % cR;
+    gk1[idx] = cscale(vh, sclR[w]);
+  }
+  __syncthreads();
+  // local_renormalize(k) and (k+1) with the new Lambda_k = s2
+  double nk = 0.0, nk1 = 0.0;
+  for (size_t idx = threadIdx.x; idx < size_t(m) * rank; idx += NT) {
+    int i = int(idx / rank), j = int(idx % rank);
+    double l = lamL[i >> 1], s = wk.s2[j];
+    cpx<T> g = gk[idx];
+    nk += (double(g.x) * g.x + double(g.y) * g.y) * (l * l) * (s * s);
+  }
+  for (size_t idx = threadIdx.x; idx < size_t(rank) * nc; idx += NT) {
+    int j = int(idx / nc), w = int(idx % nc) % cR;
+    double l = lamR[w], s = wk.s2[j];
+    cpx<T> g = gk1[idx];
+    nk1 += (double(g.x) * g.x + double(g.y) * g.y) * (s * s) * (l * l);
+  }
+  block_sum2<NT>(nk, nk1, sm.red);
+  const T ik = T(1.0 / sqrt(nk)), ik1 = T(1.0 / sqrt(nk1));
+  for (size_t idx = threadIdx.x; idx < size_t(m) * rank; idx += NT) gk[idx] = cscale(gk[idx], ik);
+  for (size_t idx = threadIdx.x; idx < size_t(rank) * nc; idx += NT) gk1[idx] = cscale(gk1[idx], ik1);
+  for (int j = threadIdx.x; j < rank; j += NT) lamM[j] = wk.s2[j];
+  if (threadIdx.x == 0) tr.chi[k + 1] = rank;
+  __syncthreads();
+}
+
+// ---------------------------------------------------------- accessors
+template <typename T>
+__device__ __forceinline__ cpx<T> *gamma_slot(const TrajDev &tr, int k) {
+  return reinterpret_cast<cpx<T> *>(tr.gamma) + size_t(k) * 2 * tr.cap * tr.cap;
+}
+__device__ __forceinline__ double *lam_slot(const TrajDev &tr, int s) { return tr.lam + size_t(s) * tr.cap; }
+
+// One bond operation on (k, k+1): gate != nullptr -> apply_unitary2, else local_refactor.
+template <typename T, int NT, int W>
+__device__ void bond_op(const TrajDev &tr, int k, const double *gate, Work<T> &wk, int max_sweeps,
+                        Smem<T, W> &sm) {
+  const int cL = tr.chi[k], cM = tr.chi[k + 1], cR = tr.chi[k + 2];
+  const int m = 2 * cL, nc = 2 * cR;
+  const bool colmode = m > nc;  // square: vectors = rows (coalesced theta stores)
+  const int ell = colmode ? m : nc, c = colmode ? nc : m;
+  cpx<T> *gk = gamma_slot<T>(tr, k), *gk1 = gamma_slot<T>(tr, k + 1);
+  const double *lamL = lam_slot(tr, k), *lamR = lam_slot(tr, k + 2);
+  double *lamM = lam_slot(tr, k + 1);
+  build_theta<T, NT, W>(gk, gk1, lamL, lamM, lamR, cL, cM, cR, gate, wk.A, colmode, sm);
+  int sw = jacobi_svd<T, NT, W>(wk.A, wk.V, ell, c, max_sweeps, sm);
+  if (sw < 0 && threadIdx.x == 0) atomicOr(tr.status, ST_NOT_CONVERGED);
+  finalize_bond<T, NT, W>(tr, k, gk, gk1, lamL, lamM, lamR, cL, cR, colmode, ell, c, wk, sm);
+}
+
+// local_probs (mps.rs:1079-1134): p_s = sum L_{k-1}[v]^2 |G[v,s,u]|^2 L_k[u]^2
+template <typename T, int NT, int W>
+__device__ void site_probs(const TrajDev &tr, int k, double &p0, double &p1, Smem<T, W> &sm) {
+  const int cL = tr.chi[k], cR = tr.chi[k + 1];
+  const cpx<T> *g = gamma_slot<T>(tr, k);
+  const double *lamL = lam_slot(tr, k), *lamR = lam_slot(tr, k + 1);
+  double a0 = 0.0, a1 = 0.0;
+  const int tot = cL * 2 * cR;
+  for (int idx = threadIdx.x; idx < tot; idx += NT) {
+    int u = idx % cR, s = (idx / cR) & 1, v = idx / (2 * cR);
+    cpx<T> x = g[idx];
+    double w = (double(x.x) * x.x + double(x.y) * x.y) * (lamL[v] * lamL[v]) * (lamR[u] * lamR[u]);
+    if (s) a1 += w; else a0 += w;
+  }
+  block_sum2<NT>(a0, a1, sm.red);
+  p0 = a0;
+  p1 = a1;
+}
+
+// sample_state + project (mps.rs:1427-1465)
+template <typename T, int NT, int W>
+__device__ void measure_site(const TrajDev &tr, int k, double u, int post, int *out_outcome, double *out_prob,
+                             Smem<T, W> &sm) {
+  double p0, p1;
+  site_probs<T, NT, W>(tr, k, p0, p1, sm);
+  int outcome;
+  if (post >= 0)
+    outcome = post;
+  else
+    outcome = (u < p0) ? 0 : 1;
+  const double prob = outcome ? p1 : p0;
+  const double sum = p0 + p1;
+  if (threadIdx.x == 0) {
+    if (out_outcome) *out_outcome = outcome;
+    if (out_prob) *out_prob = prob;
+    const double ptol = (sizeof(T) == 8) ? 1e-9 : 1e-4;
+    if (!(fabs(sum - 1.0) <= ptol)) atomicOr(tr.status, ST_PROB_SUM);
+  }
+  const int cL = tr.chi[k], cR = tr.chi[k + 1];
+  cpx<T> *g = gamma_slot<T>(tr, k);
+  const T inv = T(1.0 / sqrt(prob));
+  const int tot = cL * 2 * cR;
+  for (int idx = threadIdx.x; idx < tot; idx += NT) {
+    int s = (idx / cR) & 1;
+    g[idx] = (s == outcome) ? cscale(g[idx], inv) : czero<T>();
+  }
+  __syncthreads();
+}
+
+// apply_unitary1 (mps.rs:1298-1314): Gamma_k[v,:,u] <- op Gamma_k[v,:,u]
+template <typename T, int NT, int W>
+__device__ void unitary1(const TrajDev &tr, int k, const double *op) {
+  const int cL = tr.chi[k], cR = tr.chi[k + 1];
+  cpx<T> *g = gamma_slot<T>(tr, k);
+  cpx<T> o00 = mkc<T>(T(op[0]), T(op[1])), o01 = mkc<T>(T(op[2]), T(op[3]));
+  cpx<T> o10 = mkc<T>(T(op[4]), T(op[5])), o11 = mkc<T>(T(op[6]), T(op[7]));
+  for (int idx = threadIdx.x; idx < cL * cR; idx += NT) {
+    int v = idx / cR, u = idx % cR;
+    cpx<T> a = g[(v * 2 + 0) * cR + u], b = g[(v * 2 + 1) * cR + u];
+    g[(v * 2 + 0) * cR + u] = cfma(o01, b, cmul(o00, a));
+    g[(v * 2 + 1) * cR + u] = cfma(o11, b, cmul(o10, a));
+  }
+  __syncthreads();
+}
+
+// entropy_vn (mps.rs:1251-1261) / entropy_ry_schmidt (1268-1282), float64
+template <int NT>
+__device__ double bond_entropy(const TrajDev &tr, int b, double alpha, double *red) {
+  const int cb = tr.chi[b + 1];
+  const double *s = tr.lam + size_t(b + 1) * tr.cap;
+  double acc = 0.0;
+  for (int j = threadIdx.x; j < cb; j += NT) {
+    double s2 = s[j] * s[j];
+    if (alpha == 1.0)
+      acc += -s2 * log(s2);
+    else
+      acc += pow(s2, alpha);
+  }
+  double tot = block_sum<NT>(acc, red);
+  if (alpha == 1.0) return tot;
+  return log(tot) / (1.0 - alpha);
+}
+
+template <typename T, int NT, int W>
+__device__ void run_program(const LaunchArgs &la, const Item &it, Work<T> &wk, Smem<T, W> &sm) {
+  const TrajDev tr = la.trajs[it.traj];
+  for (int pc = 0; pc < it.len; ++pc) {
+    const Instr in = la.prog[it.off + pc];
+    switch (in.op) {
+      case OP_GATE:
+        bond_op<T, NT, W>(tr, in.k, la.gates + size_t(in.a) * 32, wk, la.max_sweeps, sm);
+        break;
+      case OP_REFACTOR:
+        bond_op<T, NT, W>(tr, in.k, nullptr, wk, la.max_sweeps, sm);
+        break;
+      case OP_MEAS:
+        measure_site<T, NT, W>(tr, in.k, la.us[in.a], in.b, la.outcomes + in.a, la.probs + in.a, sm);
+        break;
+      case OP_ENTROPY: {
+        double e = bond_entropy<NT>(tr, in.k, 1.0, sm.red);
+        if (threadIdx.x == 0) la.ents[in.a] = e;
+        __syncthreads();
+        break;
+      }
+      case OP_RENYI: {
+        double e = bond_entropy<NT>(tr, in.k, la.us[in.b], sm.red);
+        if (threadIdx.x == 0) la.ents[in.a] = e;
+        __syncthreads();
+        break;
+      }
+      case OP_UNI1:
+        unitary1<T, NT, W>(tr, in.k, la.gates + size_t(in.a) * 32);
+        break;
+      case OP_PROBS: {
+        double p0, p1;
+        site_probs<T, NT, W>(tr, in.k, p0, p1, sm);
+        if (threadIdx.x == 0) {
+          la.pout[2 * in.a] = p0;
+          la.pout[2 * in.a + 1] = p1;
+        }
+        __syncthreads();
+        break;
+      }
+      default:
+        if (threadIdx.x == 0) atomicOr(tr.status, ST_BAD_INSTR);
+        break;
+    }
+  }
+}
+
+}  // namespace tn

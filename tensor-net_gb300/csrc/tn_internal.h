@@ -1,0 +1,84 @@
+// tn_internal.h -- types shared by the host runtime and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace tn {
+
+// Threads per executor CTA and Jacobi block-pair width.
+constexpr int kThreads = 512;
+constexpr int kBlockW = 32;
+
+// Instruction set of a trajectory program (one CTA executes one program).
+enum Opcode : int {
+  OP_NOP = 0,
+  OP_GATE = 1,      // k, a = gate index          apply_unitary2 (mps.rs:1332)
+  OP_REFACTOR = 2,  // k                          local_refactor (mps.rs:846)
+  OP_MEAS = 3,      // k, a = slot, b = post|-1   sample_state+project (mps.rs:1427-1465)
+  OP_ENTROPY = 4,   // k = bond, a = slot         entropy_vn (mps.rs:1251)
+  OP_UNI1 = 5,      // k, a = gate index          apply_unitary1 (mps.rs:1298)
+  OP_PROBS = 6,     // k, a = slot                local_probs (mps.rs:1079)
+  OP_RENYI = 7      // k = bond, a = slot, b = index of alpha in us[]  entropy_ry_schmidt (mps.rs:1268)
+};
+
+struct Instr {
+  int op, k, a, b;
+};
+
+// Device error word bits (or-ed into *TrajDev::status).
+enum : int {
+  ST_NOT_CONVERGED = 1,
+  ST_CAPACITY = 2,
+  ST_PROB_SUM = 4,
+  ST_BAD_INSTR = 8,
+};
+
+struct TrajDev {
+  void *gamma;     // n slots of 2*cap*cap complex<T>
+  double *lam;     // n+1 slots of cap float64
+  int *chi;        // n+1 bond dimensions (chi[0] = chi[n] = 1)
+  int *status;     // error word
+  int n, cap;
+  int trunc_mode, chi_max;
+  double cutoff;
+};
+
+struct Item {
+  int traj, off, len, pad;
+};
+
+struct LaunchArgs {
+  const Item *items;
+  int nitems;
+  int *counter;
+  TrajDev *trajs;
+  const Instr *prog;
+  const double *gates;   // 32 doubles per gate (4x4 complex128 row-major)
+  const double *us;      // uniforms (and Renyi alphas)
+  int *outcomes;
+  double *probs;
+  double *ents;
+  double *pout;          // OP_PROBS output, 2 per slot
+  void *ws;              // per-CTA workspace
+  size_t ws_stride;      // bytes per CTA
+  int max_sweeps;
+};
+
+cudaError_t launch_run(int prec, const LaunchArgs &la, int grid, int sortP, int ws_cap, cudaStream_t st);
+size_t run_smem_bytes(int prec, int sortP);
+size_t run_work_bytes(int prec, int cap);
+int run_blocks_per_sm(int prec, int sortP);
+cudaError_t launch_reset(TrajDev *trajs, const int *list, int count, int prec, cudaStream_t st);
+cudaError_t launch_compile(const TrajDev *trajs, const int *list, int nt, const int *order, const int *gate_off,
+                           const int *gate_ks, const int *meas_off, const int *meas_ks, int pcap, Instr *prog,
+                           Item *items, cudaStream_t st);
+
+inline int next_pow2(int x) {
+  int p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+}  // namespace tn

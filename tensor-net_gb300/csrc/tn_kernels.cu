@@ -1,0 +1,151 @@
+// tn_kernels.cu -- kernels of the trajectory engine and their launchers.
+//
+//  k_run        persistent executor: CTAs pull work items (one trajectory's
+//               instruction list each) from an atomic counter and run them with
+//               the device routines of tn_device.cuh.
+//  k_compile    builds every trajectory's instruction list for one brickwork
+//               layer on the device (apply_bilayer, circuit.rs:624-659 ->
+//               apply_meas_prob_layer control flow, mps.rs:2206-2252).
+//  k_reset      re-initialises trajectory slots to |0...0> (MPS::new,
+//               mps.rs:370-391).
+#include "tn_device.cuh"
+#include "tn_internal.h"
+
+namespace tn {
+
+template <typename T, int NT, int W>
+__global__ void __launch_bounds__(NT, 1) k_run(LaunchArgs la, int sortP, int ws_cap) {
+  extern __shared__ __align__(256) unsigned char smem[];
+  __shared__ int s_item;
+  Smem<T, W> sm(smem, sortP);
+  Work<T> wk = make_work<T>(reinterpret_cast<unsigned char *>(la.ws) + size_t(blockIdx.x) * la.ws_stride, ws_cap);
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(la.counter, 1);
+    __syncthreads();
+    const int it = s_item;
+    __syncthreads();
+    if (it >= la.nitems) break;
+    run_program<T, NT, W>(la, la.items[it], wk, sm);
+  }
+}
+
+__global__ void k_reset(TrajDev *trajs, const int *list, int count, int elem_bytes) {
+  const int t = list[blockIdx.x];
+  const TrajDev tr = trajs[t];
+  const size_t slot = size_t(2) * tr.cap * tr.cap;
+  for (int k = threadIdx.x; k < tr.n; k += blockDim.x) {
+    if (elem_bytes == 16) {
+      cpx<double> *g = reinterpret_cast<cpx<double> *>(tr.gamma) + size_t(k) * slot;
+      g[0] = mkc<double>(1.0, 0.0);
+      g[1] = mkc<double>(0.0, 0.0);
+    } else {
+      cpx<float> *g = reinterpret_cast<cpx<float> *>(tr.gamma) + size_t(k) * slot;
+      g[0] = mkc<float>(1.f, 0.f);
+      g[1] = mkc<float>(0.f, 0.f);
+    }
+  }
+  for (int s = threadIdx.x; s <= tr.n; s += blockDim.x) {
+    tr.lam[size_t(s) * tr.cap] = 1.0;
+    tr.chi[s] = 1;
+  }
+}
+
+// One thread per listed trajectory.  Program of list entry i lives at
+// prog + i * pcap; items[order[i]] points at it so that the executor pulls
+// the most expensive trajectories first.
+__global__ void k_compile(const TrajDev *trajs, const int *list, int nt, const int *order, const int *gate_off,
+                          const int *gate_ks, const int *meas_off, const int *meas_ks, int pcap, Instr *prog,
+                          Item *items) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nt) return;
+  const int t = list[i];
+  const int n = trajs[t].n;
+  Instr *p = prog + size_t(i) * pcap;
+  int pc = 0;
+  auto emit = [&](int op, int k, int a, int b) {
+    if (pc < pcap) p[pc] = Instr{op, k, a, b};
+    ++pc;
+  };
+  for (int g = gate_off[i]; g < gate_off[i + 1]; ++g) {
+    const int k = gate_ks[g];
+    if (n > 1 && k >= 0 && k < n - 1) emit(OP_GATE, k, g, 0);
+  }
+  const int m0 = meas_off[i], m1 = meas_off[i + 1];
+  int last = -1;
+  for (int j = m0; j < m1; ++j) {
+    const int k = meas_ks[j];
+    if (k < 0 || k >= n || k <= last) continue;  // host guarantees sorted unique
+    if (last >= 0)
+      for (int b = last; b < k; ++b) emit(OP_REFACTOR, b, 0, 0);
+    emit(OP_MEAS, k, j, -1);
+    last = k;
+  }
+  if (last >= 0) {
+    for (int b = last; b < n - 1; ++b) emit(OP_REFACTOR, b, 0, 0);
+    for (int b = n - 3; b >= 0; --b) emit(OP_REFACTOR, b, 0, 0);
+  }
+  if (n >= 2) emit(OP_ENTROPY, n / 2 - 1, i, 0);
+  if (pc > pcap) {  // program did not fit: run nothing, flag the trajectory
+    atomicOr(trajs[t].status, ST_BAD_INSTR);
+    pc = 0;
+  }
+  items[order[i]] = Item{t, int(size_t(i) * pcap), pc, 0};
+}
+
+// ------------------------------------------------------------- launchers
+template <typename T, int NT, int W>
+static cudaError_t launch_run_t(const LaunchArgs &la, int grid, int sortP, int ws_cap, cudaStream_t st) {
+  const size_t smem = SmemLayout<T, W>::total(sortP);
+  static int configured_bytes = 0;
+  if (int(smem) > configured_bytes) {
+    cudaError_t e = cudaFuncSetAttribute(k_run<T, NT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    configured_bytes = int(smem);
+  }
+  k_run<T, NT, W><<<grid, NT, smem, st>>>(la, sortP, ws_cap);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_run(int prec, const LaunchArgs &la, int grid, int sortP, int ws_cap, cudaStream_t st) {
+  if (prec == 0) return launch_run_t<double, kThreads, kBlockW>(la, grid, sortP, ws_cap, st);
+  return launch_run_t<float, kThreads, kBlockW>(la, grid, sortP, ws_cap, st);
+}
+
+size_t run_smem_bytes(int prec, int sortP) {
+  if (prec == 0) return SmemLayout<double, kBlockW>::total(sortP);
+  return SmemLayout<float, kBlockW>::total(sortP);
+}
+
+size_t run_work_bytes(int prec, int cap) { return prec == 0 ? work_bytes<double>(cap) : work_bytes<float>(cap); }
+
+int run_blocks_per_sm(int prec, int sortP) {
+  int nb = 0;
+  const size_t smem = run_smem_bytes(prec, sortP);
+  cudaError_t e;
+  if (prec == 0) {
+    cudaFuncSetAttribute(k_run<double, kThreads, kBlockW>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_run<double, kThreads, kBlockW>, kThreads, smem);
+  } else {
+    cudaFuncSetAttribute(k_run<float, kThreads, kBlockW>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_run<float, kThreads, kBlockW>, kThreads, smem);
+  }
+  if (e != cudaSuccess || nb < 1) nb = 1;
+  return nb;
+}
+
+cudaError_t launch_reset(TrajDev *trajs, const int *list, int count, int prec, cudaStream_t st) {
+  if (count <= 0) return cudaSuccess;
+  k_reset<<<count, 128, 0, st>>>(trajs, list, count, prec == 0 ? 16 : 8);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_compile(const TrajDev *trajs, const int *list, int nt, const int *order, const int *gate_off,
+                           const int *gate_ks, const int *meas_off, const int *meas_ks, int pcap, Instr *prog,
+                           Item *items, cudaStream_t st) {
+  if (nt <= 0) return cudaSuccess;
+  k_compile<<<(nt + 127) / 128, 128, 0, st>>>(trajs, list, nt, order, gate_off, gate_ks, meas_off, meas_ks, pcap,
+                                              prog, items);
+  return cudaGetLastError();
+}
+
+}  // namespace tn

@@ -1,0 +1,242 @@
+"""Host-side mirror of tensor-net's ``MPS<Q, C64>`` over the C ABI.
+
+Method names, argument meaning and out-of-range behaviour follow
+``tensor-net/lib/mps.rs``; the state lives on the GPU (``tn_mps`` handle).
+Randomness is caller-supplied: every measurement takes the uniform the
+reference would have drawn from its ``rng`` at that point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+
+MODE_NONE, MODE_CONST, MODE_CUTOFF, MODE_BOTH = 0, 1, 2, 3
+PRECISIONS = {"f64": 0, "mixed": 1}
+
+
+@dataclass(frozen=True)
+class Trunc:
+    """``Option<BondDim<f64>>`` (mps.rs:157-166) plus the combined rule
+    ``rank = max(1, min(chi_max, #{s_j > cutoff}))`` (``Trunc.both``)."""
+
+    mode: int = MODE_NONE
+    chi_max: int = 0
+    cutoff: float = 0.0
+
+    @staticmethod
+    def none():
+        return Trunc(MODE_NONE, 0, 0.0)
+
+    @staticmethod
+    def const(r: int):
+        return Trunc(MODE_CONST, int(r), 0.0)
+
+    @staticmethod
+    def cut(eps: float):
+        return Trunc(MODE_CUTOFF, 0, float(eps))
+
+    @staticmethod
+    def both(r: int, eps: float):
+        return Trunc(MODE_BOTH, int(r), float(eps))
+
+    def c(self) -> L.tn_trunc:
+        return L.tn_trunc(int(self.mode), int(self.chi_max), float(self.cutoff))
+
+
+def _as_op(op, d: int):
+    a = np.ascontiguousarray(np.asarray(op, dtype=np.complex128))
+    if a.ndim != 2:
+        a = a.reshape(1, -1)
+    return a.view(np.float64).reshape(-1).copy(), a.shape
+
+
+class MPS:
+    """GPU-resident Schmidt-form MPS of qubits (mps.rs:339-356)."""
+
+    def __init__(self, n: int, trunc: Trunc | None = None, precision: str = "f64", chi_cap: int = 0,
+                 _handle=None):
+        self._lib = L.lib()
+        self._h = C.c_void_p()
+        if _handle is not None:
+            self._h = _handle
+        else:
+            tr = C.byref(trunc.c()) if trunc is not None else None
+            L.check(self._lib.tn_mps_new_qubits(int(n), tr, PRECISIONS[precision], int(chi_cap),
+                                                C.byref(self._h)), "tn_mps_new_qubits")
+        nn = L.u32()
+        L.check(self._lib.tn_mps_n(self._h, C.byref(nn)), "tn_mps_n")
+        self.n = int(nn.value)
+
+    @classmethod
+    def new_qubits(cls, n: int, trunc: Trunc | None = None, precision: str = "f64", chi_cap: int = 0):
+        """``MPS::new_qubits`` (mps.rs:2033-2039)."""
+        return cls(n, trunc, precision, chi_cap)
+
+    def close(self):
+        if self._h:
+            self._lib.tn_mps_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def clone(self) -> "MPS":
+        h = C.c_void_p()
+        L.check(self._lib.tn_mps_clone(self._h, C.byref(h)), "tn_mps_clone")
+        return MPS(0, _handle=h)
+
+    def get_trunc(self):
+        t = L.tn_trunc()
+        s = L.check(self._lib.tn_mps_get_trunc(self._h, C.byref(t)), "tn_mps_get_trunc")
+        return None if s == L.TN_NONE else Trunc(t.mode, t.chi_max, t.cutoff)
+
+    def set_trunc(self, trunc: Trunc | None):
+        tr = C.byref(trunc.c()) if trunc is not None else None
+        L.check(self._lib.tn_mps_set_trunc(self._h, tr), "tn_mps_set_trunc")
+
+    # ---- unitaries
+    def apply_unitary1(self, k: int, op):
+        """``apply_unitary1`` (mps.rs:1298-1314)."""
+        buf, shape = _as_op(op, 2)
+        L.check(self._lib.tn_mps_apply_unitary1(self._h, int(k), L.dptr(buf), shape[0], shape[1]),
+                "apply_unitary1")
+        return self
+
+    def apply_unitary2(self, k: int, op):
+        """``apply_unitary2`` (mps.rs:1332-1387)."""
+        buf, shape = _as_op(op, 4)
+        L.check(self._lib.tn_mps_apply_unitary2(self._h, int(k), L.dptr(buf), shape[0], shape[1]),
+                "apply_unitary2")
+        return self
+
+    # ---- probabilities / measurement
+    def probs(self, k: int):
+        """``probs`` (mps.rs:1071-1076)."""
+        out = np.zeros(2)
+        s = L.check(self._lib.tn_mps_probs(self._h, int(k), L.dptr(out)), "probs")
+        return None if s == L.TN_NONE else out
+
+    def prob(self, k: int, p: int):
+        out = L.dbl()
+        s = L.check(self._lib.tn_mps_prob(self._h, int(k), int(p), C.byref(out)), "prob")
+        return None if s == L.TN_NONE else out.value
+
+    def measure_prob(self, k: int, u: float):
+        """``measure_prob`` (mps.rs:1479-1489) with the uniform ``u``."""
+        oc, pr = L.i32(), L.dbl()
+        s = L.check(self._lib.tn_mps_measure_prob(self._h, int(k), float(u), C.byref(oc), C.byref(pr)),
+                    "measure_prob")
+        return None if s == L.TN_NONE else (int(oc.value), float(pr.value))
+
+    def measure(self, k: int, u: float):
+        r = self.measure_prob(k, u)
+        return None if r is None else r[0]
+
+    def measure_postsel_prob(self, k: int, p: int):
+        """``measure_postsel_prob`` (mps.rs:1501-1510)."""
+        pr = L.dbl()
+        s = L.check(self._lib.tn_mps_measure_postsel_prob(self._h, int(k), int(p), C.byref(pr)),
+                    "measure_postsel_prob")
+        return None if s == L.TN_NONE else float(pr.value)
+
+    def measure_postsel(self, k: int, p: int):
+        self.measure_postsel_prob(k, p)
+
+    def apply_meas_prob_layer(self, ks, us=None, posts=None):
+        """``apply_meas_prob_layer`` (mps.rs:2206-2252): list of (k, outcome, prob)."""
+        ks = np.ascontiguousarray(np.asarray(ks, dtype=np.uint32).reshape(-1))
+        nk = ks.size
+        usa = None if us is None else np.ascontiguousarray(np.asarray(us, dtype=np.float64).reshape(-1))
+        pa = None if posts is None else np.ascontiguousarray(np.asarray(posts, dtype=np.int32).reshape(-1))
+        if usa is not None and usa.size < nk:
+            usa = np.concatenate([usa, np.zeros(nk - usa.size)])
+        ok = np.zeros(max(nk, 1), np.uint32)
+        oc = np.zeros(max(nk, 1), np.int32)
+        pr = np.zeros(max(nk, 1), np.float64)
+        nout = L.u32()
+        L.check(self._lib.tn_mps_apply_meas_prob_layer(self._h, L.uptr(ks), nk, L.iptr(pa), L.dptr(usa),
+                                                       L.uptr(ok), L.iptr(oc), L.dptr(pr), C.byref(nout)),
+                "apply_meas_prob_layer")
+        m = nout.value
+        return [(int(ok[j]), int(oc[j]), float(pr[j])) for j in range(m)]
+
+    def apply_bilayer(self, gate_ks, gates, meas_ks, us):
+        """``circuit::apply_bilayer`` (circuit.rs:624-659), one device launch."""
+        gk = np.ascontiguousarray(np.asarray(gate_ks, dtype=np.uint32).reshape(-1))
+        g = np.ascontiguousarray(np.asarray(gates, dtype=np.complex128).reshape(-1, 4, 4))
+        gbuf = g.view(np.float64).reshape(-1).copy() if g.size else np.zeros(1)
+        mk = np.ascontiguousarray(np.asarray(meas_ks, dtype=np.uint32).reshape(-1))
+        u = np.ascontiguousarray(np.asarray(us, dtype=np.float64).reshape(-1))
+        if u.size < mk.size:
+            u = np.concatenate([u, np.zeros(mk.size - u.size)])
+        nm = mk.size
+        ok = np.zeros(max(nm, 1), np.uint32)
+        oc = np.zeros(max(nm, 1), np.int32)
+        pr = np.zeros(max(nm, 1), np.float64)
+        nout = L.u32()
+        L.check(self._lib.tn_mps_apply_bilayer(self._h, L.uptr(gk), L.dptr(gbuf), gk.size, L.uptr(mk), nm,
+                                               L.dptr(u if u.size else np.zeros(1)), L.uptr(ok), L.iptr(oc),
+                                               L.dptr(pr), C.byref(nout)), "apply_bilayer")
+        return [(int(ok[j]), int(oc[j]), float(pr[j])) for j in range(nout.value)]
+
+    # ---- entropies and bonds
+    def entropy_vn(self, b: int):
+        """``entropy_vn`` (mps.rs:1251-1261)."""
+        out = L.dbl()
+        s = L.check(self._lib.tn_mps_entropy_vn(self._h, int(b), C.byref(out)), "entropy_vn")
+        return None if s == L.TN_NONE else float(out.value)
+
+    def entropy_ry_schmidt(self, a: float, b: int):
+        """``entropy_ry_schmidt`` (mps.rs:1268-1282)."""
+        out = L.dbl()
+        s = L.check(self._lib.tn_mps_entropy_ry_schmidt(self._h, float(a), int(b), C.byref(out)),
+                    "entropy_ry_schmidt")
+        return None if s == L.TN_NONE else float(out.value)
+
+    def bond_dim(self, b: int):
+        out = L.u32()
+        s = L.check(self._lib.tn_mps_bond_dim(self._h, int(b), C.byref(out)), "bond_dim")
+        return None if s == L.TN_NONE else int(out.value)
+
+    def max_bond_dim(self):
+        out = L.u32()
+        s = L.check(self._lib.tn_mps_max_bond_dim(self._h, C.byref(out)), "max_bond_dim")
+        return None if s == L.TN_NONE else int(out.value)
+
+    def svals(self, b: int):
+        ln = L.u32()
+        s = L.check(self._lib.tn_mps_svals(self._h, int(b), None, 0, C.byref(ln)), "svals")
+        if s == L.TN_NONE:
+            return None
+        out = np.zeros(max(1, ln.value))
+        L.check(self._lib.tn_mps_svals(self._h, int(b), L.dptr(out), out.size, C.byref(ln)), "svals")
+        return out[: ln.value]
+
+    def gamma(self, k: int):
+        """Gamma_k in the reference layout (chi_{k-1}, 2, chi_k), complex128."""
+        dims = (L.u32 * 3)()
+        s = L.check(self._lib.tn_mps_export_gamma(self._h, int(k), None, 0, dims), "export_gamma")
+        if s == L.TN_NONE:
+            return None
+        shape = (dims[0], dims[1], dims[2])
+        out = np.zeros(2 * shape[0] * shape[1] * shape[2])
+        L.check(self._lib.tn_mps_export_gamma(self._h, int(k), L.dptr(out), out.size, dims), "export_gamma")
+        return out.view(np.complex128).reshape(shape)
+
+    def contract(self):
+        """``contract`` (mps.rs:794-798): dense state vector (n <= 24)."""
+        out = np.zeros(2 * (1 << self.n))
+        L.check(self._lib.tn_mps_contract(self._h, L.dptr(out), out.size), "contract")
+        return out.view(np.complex128)
+
+    def device_status(self) -> int:
+        st = L.i32()
+        L.check(self._lib.tn_mps_device_status(self._h, C.byref(st)), "device_status")
+        return int(st.value)
