@@ -1,0 +1,429 @@
+"""Benchmark of the GB300 MPS trajectory engine: trajectory-layers per second.
+
+Workload (one "step" = one brickwork layer of every trajectory in the batch):
+N=64 qubits, chi_max=256, singular-value cutoff 1e-10, Haar-random U(4)
+gates, each qubit Z-measured with probability p (p cycles over
+0.05/0.10/0.15/0.20/0.30 across trajectories), half-chain entropy read after
+each layer; seeded synthetic inputs (counter-based generator, identical arrays
+for every implementation).  The batch first evolves `--prefill` layers
+untimed from |0...0> so that the timed layers run in the entangled regime.
+
+Lines printed (rank 0): one JSON object per run.
+  value     traj-layers/s with the layer inputs already in HBM (device
+            pointers, one persistent launch per layer), CUDA events on the
+            batch stream, max over ranks;
+  e2e       the same through the C ABI (tn_batch_step) with host buffers:
+            pinned H2D of the layer inputs and D2H of outcomes/probabilities/
+            entropies inside the timed region;
+  roofline  algorithmic flops (theta GEMM + Golub-Reinsch SVD count of every
+            bond operation, counted on the device) per launch / launch time;
+  cpu_baseline  the FP64 oracle (numpy + LAPACK gesvd) on the host cores on a
+            bounded sample of the same layers.
+`--impl reference` runs only the CPU oracle arm (the reference itself is Rust
+and cannot be built on these machines) and prints its line with
+"impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+P_LIST = (0.05, 0.10, 0.15, 0.20, 0.30)
+METRIC = "traj-layers/s & p50/p99 latency: served vs plain GPU at entropy err ≤1e-6"
+UNIT = "traj-layers/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--batch", type=int, default=0, help="trajectories per GPU (0: one per resident CTA)")
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--chi", type=int, default=256)
+    ap.add_argument("--cutoff", type=float, default=1e-10)
+    ap.add_argument("--prefill", type=int, default=10)
+    ap.add_argument("--prec", default="mixed", choices=["mixed", "f64"])
+    ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ helpers
+def p_of(traj: int) -> float:
+    return P_LIST[traj % len(P_LIST)]
+
+
+def saturated_dims(n: int, chi: int):
+    """Bond dimensions of a saturated chain: chi_b = min(chi, 2^min(b+1, n-1-b))."""
+    return [min(chi, 2 ** min(b + 1, n - 1 - b)) if min(b + 1, n - 1 - b) < 30 else chi for b in range(n - 1)]
+
+
+def op_flops(cl, cm, cr, gate):
+    """Algorithmic flops of one bond operation (theta GEMM + SVD count)."""
+    a, b = max(2 * cl, 2 * cr), min(2 * cl, 2 * cr)
+    return 8.0 * (2 * cl) * cm * (2 * cr) + (128.0 * cl * cr if gate else 0.0) + \
+        4.0 * (4 * a * a * b + 8 * a * b * b + 9 * b ** 3)
+
+
+def layer_ops(n, gate_ks, meas_ks):
+    """The bond-operation list of one apply_bilayer (mps.rs:2206-2252)."""
+    ops = [(int(k), True) for k in gate_ks]
+    ms = sorted(set(int(k) for k in meas_ks))
+    if ms:
+        last = None
+        for k in ms:
+            if last is not None:
+                ops += [(b, False) for b in range(last, k)]
+            last = k
+        ops += [(b, False) for b in range(last, n - 1)]
+        ops += [(b, False) for b in range(n - 3, -1, -1)]
+    return ops
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = pathlib.Path(os.environ.get("TMPDIR", "/tmp")) / f"tn_clocks_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        try:
+            self.path.unlink()
+        except Exception:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return d, "measured"
+        except Exception:
+            pass
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM traffic of the executor kernel from the committed ncu
+    summary (profiles/k_run_traffic.json), scaled by algorithmic bytes."""
+    p = ROOT / "profiles" / "k_run_traffic.json"
+    if not p.exists():
+        return None
+    try:
+        return json.loads(p.read_text())
+    except Exception:
+        return None
+
+
+# ----------------------------------------------------------- CPU (oracle)
+def _cpu_worker(args):
+    """Run the op list of one trajectory layer on a random saturated Vidal
+    MPS with the FP64 oracle until the time budget is spent; return
+    (elapsed, flops_done, flops_total)."""
+    import numpy as np
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    from oracle import mps_ref as R
+    n, chi, cutoff, ops, gates, budget, seed = args
+    rng = np.random.default_rng(seed)
+    dims = saturated_dims(n, chi)
+    m = R.MPS(n, R.Trunc.both(chi, cutoff))
+    full = [1] + dims + [1]
+    for k in range(n):
+        g = rng.normal(size=(full[k], 2, full[k + 1])) + 1j * rng.normal(size=(full[k], 2, full[k + 1]))
+        m.data[k] = g / np.linalg.norm(g)
+    for b in range(n - 1):
+        s = np.sort(rng.random(dims[b]))[::-1] + 1e-3
+        m.svals[b] = s / np.linalg.norm(s)
+    tot = sum(op_flops(full[k], full[k + 1], full[k + 2], gt) for k, gt in ops)
+    done = 0.0
+    gi = 0
+    t0 = time.perf_counter()
+    for k, is_gate in ops:
+        if time.perf_counter() - t0 > budget:
+            break
+        cl, cm, cr = m.data[k].shape[0], m.data[k].shape[2], m.data[k + 1].shape[2]
+        if is_gate:
+            m.apply_unitary2(k, gates[gi % len(gates)])
+            gi += 1
+        else:
+            m.local_refactor(k)
+        done += op_flops(cl, cm, cr, is_gate)
+    return time.perf_counter() - t0, done, tot
+
+
+def cpu_baseline(n, chi, cutoff, layers_by_traj, budget, cores=None):
+    """Oracle throughput on the host cores: one process per core (spawn, one
+    BLAS thread each, the reference's rayon-over-trajectories pattern), each
+    running the op list of one trajectory layer of the timed layers on a
+    saturated state for `budget` seconds; the traj-layer time is extrapolated
+    from the fraction of the layer's algorithmic flops completed."""
+    import multiprocessing as mp
+    import numpy as np
+    if cores is None:
+        cores = len(os.sched_getaffinity(0))
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    os.environ["OMP_NUM_THREADS"] = "1"
+    jobs = []
+    for i in range(cores):
+        gk, g, mk, us = layers_by_traj[i % len(layers_by_traj)]
+        ops = layer_ops(n, gk, mk)
+        jobs.append((n, chi, cutoff, ops, [np.asarray(x) for x in g] or [np.eye(4, dtype=complex)], budget, 1000 + i))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_worker, jobs)
+    per_layer = [el / (done / tot) for el, done, tot in res if done > 0]
+    layer_s = statistics.mean(per_layer)
+    value = cores / layer_s
+    return {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": (f"FP64 oracle (numpy, LAPACK gesvd, 1 BLAS thread/process) on {cores} processes, each "
+                       f"running the bond-op list of one timed traj-layer (N={n}, chi_max={chi}, saturated "
+                       f"bond dims) for {budget:.0f} s; traj-layer time extrapolated from the fraction of its "
+                       f"algorithmic flops completed ({statistics.mean([d / t for _, d, t in res]):.3f} avg)"),
+            "seconds_per_traj_layer": layer_s}
+
+
+# --------------------------------------------------------------- GPU arm
+def run_gpu(a, rank, world, local_rank):
+    import numpy as np
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    torch.cuda.set_device(local_rank)
+    lib = pkg.lib()
+    import ctypes
+    name = ctypes.create_string_buffer(128)
+    sms = ctypes.c_uint32()
+    pkg._lib.check(lib.tn_device_info(name, 128, ctypes.byref(sms)), "tn_device_info")
+    B = a.batch or int(sms.value)
+    n, chi = a.n, a.chi
+    trunc = pkg.Trunc.both(chi, a.cutoff)
+    batch = pkg.Batch([n] * B, [trunc] * B, a.prec)
+    traj0 = rank * B
+    total_layers = a.prefill + a.warmup + 2 * a.steps
+
+    def layer_inputs(t):
+        return [pkg.gen_layer(a.seed, traj0 + i, t, n, p_of(traj0 + i)) for i in range(B)]
+
+    trajs = list(range(B))
+    # prefill (untimed): evolve from |0...0>
+    for t in range(a.prefill):
+        batch.step(trajs, layer_inputs(t))
+    # stage W + K layers of inputs in HBM
+    dev = torch.device("cuda", local_rank)
+    staged = []
+    order = None
+    for t in range(a.prefill, a.prefill + a.warmup + a.steps):
+        pk = batch.pack(trajs, layer_inputs(t))
+        nm = int(pk["meas_off"][-1])
+        if order is None:
+            order = torch.arange(B, dtype=torch.int32, device=dev)
+        staged.append(dict(
+            trajs=torch.as_tensor(pk["trajs"].astype(np.int32), device=dev),
+            gate_off=torch.as_tensor(pk["gate_off"].astype(np.int32), device=dev),
+            gate_ks=torch.as_tensor(np.maximum(pk["gate_ks"], 0).astype(np.int32), device=dev),
+            gates=torch.as_tensor(pk["gates"], device=dev),
+            meas_off=torch.as_tensor(pk["meas_off"].astype(np.int32), device=dev),
+            meas_ks=torch.as_tensor(pk["meas_ks"].astype(np.int32), device=dev) if nm else
+            torch.zeros(1, dtype=torch.int32, device=dev),
+            us=torch.as_tensor(pk["us"], device=dev) if nm else torch.zeros(1, dtype=torch.float64, device=dev),
+            outc=torch.zeros(max(nm, 1), dtype=torch.int32, device=dev),
+            probs=torch.zeros(max(nm, 1), dtype=torch.float64, device=dev),
+            ents=torch.zeros(B, dtype=torch.float64, device=dev)))
+    stream = torch.cuda.ExternalStream(batch.stream(), device=dev)
+
+    def launch(s):
+        batch.step_ptrs(B, s["trajs"].data_ptr(), order.data_ptr(), s["gate_off"].data_ptr(),
+                        s["gate_ks"].data_ptr(), s["gates"].data_ptr(), s["meas_off"].data_ptr(),
+                        s["meas_ks"].data_ptr(), s["us"].data_ptr(), s["outc"].data_ptr(),
+                        s["probs"].data_ptr(), s["ents"].data_ptr())
+
+    for s in staged[: a.warmup]:
+        launch(s)
+    batch.synchronize()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    batch.stats(reset=True)
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps + 1)]
+    with torch.cuda.stream(stream):
+        evs[0].record(stream)
+        for i, s in enumerate(staged[a.warmup:]):
+            launch(s)
+            evs[i + 1].record(stream)
+    batch.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    step_ms = [evs[i].elapsed_time(evs[i + 1]) for i in range(a.steps)]
+    elapsed = sum(step_ms) / 1e3
+    st = batch.stats(reset=True)
+    status = batch.device_status()
+    if world > 1:
+        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = world * B * a.steps / elapsed
+    ents = staged[-1]["ents"].cpu().numpy()
+
+    # e2e: the C ABI with host buffers (pinned staging, H2D + launch + D2H per step)
+    e2e_layers = [layer_inputs(t) for t in range(a.prefill + a.warmup + a.steps,
+                                                   a.prefill + a.warmup + 2 * a.steps)]
+    packs = [batch.pack(trajs, L_) for L_ in e2e_layers]
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for pk in packs:
+        batch.step_packed(pk)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = statistics.mean(int(pk["gates"].nbytes + pk["us"].nbytes + 4 * (pk["gate_ks"].size + pk["meas_ks"].size +
+                                                                         2 * B + 2 * (B + 1))) for pk in packs)
+    d2h = statistics.mean(int(int(pk["meas_off"][-1]) * (4 + 8) + 8 * B) for pk in packs)
+    dims = [batch.bond_dims(i) for i in range(min(B, 5))]
+    return dict(value=value, elapsed=elapsed, step_ms=step_ms, stats=st, status=status, clocks=clk,
+                e2e=world * B * a.steps / e2e_s, h2d=h2d, d2h=d2h, B=B, gpu=name.value.decode(),
+                ents=ents, dims=dims, sms=int(sms.value), layer_inputs=layer_inputs)
+
+
+def main():
+    a = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    config = {"workload": f"N={a.n} chi_max={a.chi} cutoff={a.cutoff:g} Haar brickwork, p cycling "
+                          f"{list(P_LIST)}, layers [{a.prefill + a.warmup}, {a.prefill + a.warmup + a.steps}) "
+                          f"after {a.prefill} untimed prefill layers",
+              "n_qubits": a.n, "chi_max": a.chi, "cutoff": a.cutoff, "prefill_layers": a.prefill,
+              "precision": a.prec, "l2": "state larger than L2 (no flush needed)"}
+
+    if a.impl == "reference":
+        if rank != 0:
+            return
+        import numpy as np
+        sys.path.insert(0, str(ROOT))
+        import __graft_entry__ as ge
+        pkg = ge.load_package()
+        t = a.prefill + a.warmup
+        layers = [pkg.gen_layer(a.seed, i, t, a.n, p_of(i)) for i in range(16)]
+        steps = []
+        for _ in range(a.warmup + a.steps):
+            steps.append(cpu_baseline(a.n, a.chi, a.cutoff, layers, max(3.0, a.cpu_seconds / 2)))
+        cb = steps[-1]
+        vals = [s["value"] for s in steps[a.warmup:]]
+        v = statistics.mean(vals)
+        out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus,
+               "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 / v if v else None,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+               "data": "synthetic (seeded Haar gates and measurement uniforms)", "config": config,
+               "cpu_baseline": {"value": v, "unit": UNIT, "cores": cb["cores"], "kind": "port",
+                                "sample": cb["sample"]},
+               "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+               "note": "the reference is Rust (tensor-net); no Rust toolchain on these machines, so the "
+                       "reference arm is its FP64 restatement (oracle/mps_ref.py) on the host cores"}
+        print(json.dumps(out), flush=True)
+        return
+
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    r = run_gpu(a, rank, world, local_rank)
+    peaks, peaks_kind = measured_peaks()
+    flops = r["stats"]["flop_theta"] + r["stats"]["flop_svd"]
+    per_launch = flops / a.steps
+    launch_s = r["elapsed"] / a.steps
+    achieved = per_launch / launch_s / 1e12
+    peak = float(peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops"))
+    tr = ncu_traffic()
+    sm_mhz = r["clocks"].get("sm_mhz") or 2070.0
+    simt_peak = r["sms"] * 128 * 2 * sm_mhz * 1e6 / 1e12
+    out = {
+        "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": r["elapsed"] / a.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64+f64" if a.prec == "mixed" else "c128",
+        "data": "synthetic (seeded Haar gates and measurement uniforms)",
+        "config": dict(config, batch_per_gpu=r["B"], gpu=r["gpu"]),
+        "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
+        "gpu_launches": 2 * a.steps,
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "peak_kind": f"{peaks_kind} bf16 sustained",
+                     "traffic": (tr["bytes_per_launch_scale"] * r["stats"]["bytes"] / a.steps) if tr else None,
+                     "algorithmic_flops_per_launch": per_launch,
+                     "simt_fp32": {"peak_tflops_nominal": simt_peak, "frac": achieved / simt_peak},
+                     "kernel": "k_run (theta build + Jacobi SVD + truncation + measurement, one CTA per trajectory)"},
+        "clocks": r["clocks"],
+        "work": {"bond_ops_per_step": r["stats"]["bond_ops"] / a.steps,
+                 "jacobi_sweeps_per_op": r["stats"]["sweeps"] / max(1.0, r["stats"]["bond_ops"]),
+                 "meas_per_step": r["stats"]["meas"] / a.steps, "step_ms": r["step_ms"],
+                 "device_status": r["status"], "middle_bond_dims": [int(d[a.n // 2 - 1]) for d in r["dims"]]},
+    }
+    if rank == 0 and world == 1 and not a.no_cpu:
+        t = a.prefill + a.warmup
+        layers = [r["layer_inputs"](t)[i] for i in range(min(r["B"], 16))]
+        cb = cpu_baseline(a.n, a.chi, a.cutoff, layers, a.cpu_seconds)
+        out["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -164,6 +164,12 @@ int tn_mps_contract(const tn_mps *m, double *out, uint64_t cap);
 /* Device-side error word accumulated by this handle's kernels (0 if none);
  * cleared on read. */
 int tn_mps_device_status(tn_mps *m, int32_t *status);
+/* Work counters accumulated on the device since the last reset, 8 doubles:
+ * [0] theta flops 8*(2chiL)*chiM*(2chiR) (+128*chiL*chiR per gate),
+ * [1] SVD flops 4*(4a^2b + 8ab^2 + 9b^3) (a, b = larger/smaller side of theta),
+ * [2] bond operations, [3] Jacobi sweeps, [4] measurements,
+ * [5] algorithmic HBM bytes, [6..7] reserved.  reset != 0 zeroes them. */
+int tn_mps_stats(tn_mps *m, double *out, int32_t reset);
 
 /* ==================== batch of trajectories (batching) ==================== */
 
@@ -199,12 +205,24 @@ int tn_batch_device_inputs(tn_batch *b, uint32_t max_gates, uint32_t max_meas,
                            void **d_us, void **d_outcomes, void **d_probs,
                            void **d_entropy);
 int tn_batch_step_device(tn_batch *b, uint32_t nt);
+/* Same layer with every array supplied by the caller in device memory
+ * (int32 indices, float64 gates/uniforms): trajs[nt], order[nt] (execution
+ * rank of each entry: a permutation of 0..nt-1, 0 runs first), gate_off[nt+1],
+ * gate_ks[], gates[32 per gate], meas_off[nt+1], meas_ks[], us[], and outputs
+ * outcomes[], probs[], entropy[nt].  Stream-ordered on the batch stream, no
+ * synchronisation, no host copies. */
+int tn_batch_step_ptrs(tn_batch *b, uint32_t nt, const void *d_trajs, const void *d_order,
+                       const void *d_gate_off, const void *d_gate_ks, const void *d_gates,
+                       const void *d_meas_off, const void *d_meas_ks, const void *d_us,
+                       void *d_outcomes, void *d_probs, void *d_entropy);
 int tn_batch_synchronize(tn_batch *b);
 /* Per-trajectory queries (same meaning as the tn_mps_* ones). */
 int tn_batch_bond_dims(tn_batch *b, uint32_t t, uint32_t *out, uint32_t cap);
 int tn_batch_svals(tn_batch *b, uint32_t t, uint32_t bond, double *out, uint32_t cap,
                    uint32_t *len);
 int tn_batch_device_status(tn_batch *b, int32_t *status);
+/* Sum of the work counters (see tn_mps_stats) over all trajectories. */
+int tn_batch_stats(tn_batch *b, double *out, int32_t reset);
 /* Device bytes held by slot t (its footprint for admission control). */
 int tn_batch_slot_bytes(tn_batch *b, uint32_t t, uint64_t *bytes);
 /* Stream the batch launches on (a cudaStream_t), for callers that time with

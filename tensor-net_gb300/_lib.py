@@ -56,6 +56,7 @@ SIGNATURES = {
     "tn_mps_export_gamma": (C.c_int, [vp, u32, P(dbl), u64, P(u32)]),
     "tn_mps_contract": (C.c_int, [vp, P(dbl), u64]),
     "tn_mps_device_status": (C.c_int, [vp, P(i32)]),
+    "tn_mps_stats": (C.c_int, [vp, P(dbl), i32]),
     "tn_batch_create": (C.c_int, [u32, P(u32), P(tn_trunc), i32, P(u32), P(vp)]),
     "tn_batch_free": (C.c_int, [vp]),
     "tn_batch_reset": (C.c_int, [vp, u32, u32, P(tn_trunc)]),
@@ -63,6 +64,8 @@ SIGNATURES = {
                                 P(i32), P(dbl), P(dbl)]),
     "tn_batch_device_inputs": (C.c_int, [vp, u32, u32] + [P(vp)] * 10),
     "tn_batch_step_device": (C.c_int, [vp, u32]),
+    "tn_batch_step_ptrs": (C.c_int, [vp, u32] + [vp] * 11),
+    "tn_batch_stats": (C.c_int, [vp, P(dbl), i32]),
     "tn_batch_synchronize": (C.c_int, [vp]),
     "tn_batch_bond_dims": (C.c_int, [vp, u32, P(u32), u32]),
     "tn_batch_svals": (C.c_int, [vp, u32, u32, P(dbl), u32, P(u32)]),

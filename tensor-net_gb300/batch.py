@@ -108,6 +108,16 @@ class Batch:
         L.check(self._lib.tn_batch_device_status(self._h, C.byref(st)), "device_status")
         return int(st.value)
 
+    def stats(self, reset: bool = False):
+        out = np.zeros(8)
+        L.check(self._lib.tn_batch_stats(self._h, L.dptr(out), int(reset)), "stats")
+        return dict(flop_theta=out[0], flop_svd=out[1], bond_ops=out[2], sweeps=out[3], meas=out[4], bytes=out[5])
+
+    def step_ptrs(self, nt, trajs, order, gate_off, gate_ks, gates, meas_off, meas_ks, us, outcomes, probs, entropy):
+        """Layer step from device pointers (ints: int32, reals: float64)."""
+        L.check(self._lib.tn_batch_step_ptrs(self._h, int(nt), trajs, order, gate_off, gate_ks, gates, meas_off,
+                                             meas_ks, us, outcomes, probs, entropy), "tn_batch_step_ptrs")
+
     def slot_bytes(self, t: int) -> int:
         b = L.u64()
         L.check(self._lib.tn_batch_slot_bytes(self._h, int(t), C.byref(b)), "slot_bytes")

@@ -57,6 +57,7 @@ struct tn_batch {
   void *arena = nullptr;
   TrajDev *dtraj = nullptr;
   int *dstatus = nullptr;
+  double *dstats = nullptr;
   void *ws = nullptr;
   size_t ws_stride = 0;
   // step buffers: one packed device block + one pinned host block
@@ -127,12 +128,32 @@ int ensure_step(tn_batch *b, uint32_t nt, uint32_t ng, uint32_t nm) {
   return TN_OK;
 }
 
-int launch_step(tn_batch *b, uint32_t nt, const StepLayout &L, char *dbase) {
-  const int *list = reinterpret_cast<const int *>(dbase + L.list);
-  const int *order = reinterpret_cast<const int *>(dbase + L.order);
-  CKB(launch_compile(b->dtraj, list, int(nt), order, reinterpret_cast<const int *>(dbase + L.goff),
-                     reinterpret_cast<const int *>(dbase + L.gks), reinterpret_cast<const int *>(dbase + L.moff),
-                     reinterpret_cast<const int *>(dbase + L.mks), b->pcap, b->dprog, b->ditems, b->st));
+struct StepPtrs {
+  const int *list, *order, *goff, *gks, *moff, *mks;
+  const double *gates, *us;
+  int *outc;
+  double *probs, *ents;
+};
+
+StepPtrs ptrs_of(const StepLayout &L, char *dbase) {
+  StepPtrs p;
+  p.list = reinterpret_cast<const int *>(dbase + L.list);
+  p.order = reinterpret_cast<const int *>(dbase + L.order);
+  p.goff = reinterpret_cast<const int *>(dbase + L.goff);
+  p.gks = reinterpret_cast<const int *>(dbase + L.gks);
+  p.moff = reinterpret_cast<const int *>(dbase + L.moff);
+  p.mks = reinterpret_cast<const int *>(dbase + L.mks);
+  p.gates = reinterpret_cast<const double *>(dbase + L.gates);
+  p.us = reinterpret_cast<const double *>(dbase + L.us);
+  p.outc = reinterpret_cast<int *>(dbase + L.outc);
+  p.probs = reinterpret_cast<double *>(dbase + L.probs);
+  p.ents = reinterpret_cast<double *>(dbase + L.ents);
+  return p;
+}
+
+int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P) {
+  CKB(launch_compile(b->dtraj, P.list, int(nt), P.order, P.goff, P.gks, P.moff, P.mks, b->pcap, b->dprog, b->ditems,
+                     b->st));
   CKB(cudaMemsetAsync(b->dcounter, 0, sizeof(int), b->st));
   LaunchArgs la{};
   la.items = b->ditems;
@@ -140,12 +161,12 @@ int launch_step(tn_batch *b, uint32_t nt, const StepLayout &L, char *dbase) {
   la.counter = b->dcounter;
   la.trajs = b->dtraj;
   la.prog = b->dprog;
-  la.gates = reinterpret_cast<const double *>(dbase + L.gates);
-  la.us = reinterpret_cast<const double *>(dbase + L.us);
-  la.outcomes = reinterpret_cast<int *>(dbase + L.outc);
-  la.probs = reinterpret_cast<double *>(dbase + L.probs);
-  la.ents = reinterpret_cast<double *>(dbase + L.ents);
-  la.pout = reinterpret_cast<double *>(dbase + L.probs);
+  la.gates = P.gates;
+  la.us = P.us;
+  la.outcomes = P.outc;
+  la.probs = P.probs;
+  la.ents = P.ents;
+  la.pout = P.probs;
   la.ws = b->ws;
   la.ws_stride = b->ws_stride;
   la.max_sweeps = 40;
@@ -204,9 +225,11 @@ int tn_batch_create(uint32_t ntraj, const uint32_t *ns, const tn_trunc *truncs, 
   if (e != cudaSuccess) return bail(fail(e, "cudaStreamCreate"));
   e = cudaMalloc(&b->arena, std::max<size_t>(total, 256));
   if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(arena)"));
-  e = cudaMalloc(reinterpret_cast<void **>(&b->dtraj), sizeof(TrajDev) * ntraj + sizeof(int) * (ntraj + 2));
+  e = cudaMalloc(reinterpret_cast<void **>(&b->dtraj), sizeof(TrajDev) * ntraj + sizeof(double) * STAT_N * ntraj +
+                                                        sizeof(int) * (ntraj + 2));
   if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(traj)"));
-  b->dstatus = reinterpret_cast<int *>(b->dtraj + ntraj);
+  b->dstats = reinterpret_cast<double *>(b->dtraj + ntraj);
+  b->dstatus = reinterpret_cast<int *>(b->dstats + STAT_N * ntraj);
   b->dcounter = b->dstatus + ntraj;
   for (uint32_t i = 0; i < ntraj; ++i) {
     TrajDev &d = b->h[i];
@@ -216,6 +239,7 @@ int tn_batch_create(uint32_t ntraj, const uint32_t *ns, const tn_trunc *truncs, 
     d.lam = reinterpret_cast<double *>(base + align256(size_t(2) * c * c * eb * n));
     d.chi = reinterpret_cast<int *>(reinterpret_cast<char *>(d.lam) + align256(sizeof(double) * size_t(c) * (n + 1)));
     d.status = b->dstatus + i;
+    d.stats = b->dstats + size_t(STAT_N) * i;
     d.n = int(n);
     d.cap = int(c);
     if (truncs) {
@@ -230,6 +254,7 @@ int tn_batch_create(uint32_t ntraj, const uint32_t *ns, const tn_trunc *truncs, 
   }
   e = cudaMemcpyAsync(b->dtraj, b->h.data(), sizeof(TrajDev) * ntraj, cudaMemcpyHostToDevice, b->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(b->dstatus, 0, sizeof(int) * (ntraj + 2), b->st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->dstats, 0, sizeof(double) * STAT_N * ntraj, b->st);
   if (e != cudaSuccess) return bail(fail(e, "init"));
   int dev = 0;
   cudaGetDevice(&dev);
@@ -353,7 +378,7 @@ int tn_batch_step(tn_batch *b, const uint32_t *trajs, uint32_t nt, const uint32_
   if (ng) std::memcpy(hb + L.gates, gates, sizeof(double) * 32 * ng);
   if (nm) std::memcpy(hb + L.us, us, sizeof(double) * nm);
   CKB(cudaMemcpyAsync(b->dstep, b->hstep, L.in_bytes, cudaMemcpyHostToDevice, b->st));
-  if (int s = launch_step(b, nt, L, reinterpret_cast<char *>(b->dstep))) return s;
+  if (int s = launch_step(b, nt, ptrs_of(L, reinterpret_cast<char *>(b->dstep)))) return s;
   const size_t out_bytes = L.total - L.out_off;
   CKB(cudaMemcpyAsync(hb + L.out_off, reinterpret_cast<char *>(b->dstep) + L.out_off, out_bytes,
                       cudaMemcpyDeviceToHost, b->st));
@@ -406,7 +431,7 @@ int tn_batch_step_device(tn_batch *b, uint32_t nt) {
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ge = nullptr;
     CKB(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
-    int s = launch_step(b, nt, L, reinterpret_cast<char *>(b->din));
+    int s = launch_step(b, nt, ptrs_of(L, reinterpret_cast<char *>(b->din)));
     cudaError_t e = cudaStreamEndCapture(b->st, &g);
     if (s != TN_OK) {
       if (g) cudaGraphDestroy(g);
@@ -419,6 +444,42 @@ int tn_batch_step_device(tn_batch *b, uint32_t nt) {
     it = b->graphs.emplace(nt, ge).first;
   }
   CKB(cudaGraphLaunch(it->second, b->st));
+  return TN_OK;
+}
+
+int tn_batch_step_ptrs(tn_batch *b, uint32_t nt, const void *d_trajs, const void *d_order, const void *d_gate_off,
+                       const void *d_gate_ks, const void *d_gates, const void *d_meas_off, const void *d_meas_ks,
+                       const void *d_us, void *d_outcomes, void *d_probs, void *d_entropy) {
+  if (!b || nt > b->ntraj || !d_trajs || !d_order || !d_gate_off || !d_meas_off || !d_entropy)
+    return TN_ERR_INVALID_ARG;
+  if (nt == 0) return TN_OK;
+  if (int s = ensure_step(b, b->ntraj, 1, 1)) return s;
+  StepPtrs P;
+  P.list = static_cast<const int *>(d_trajs);
+  P.order = static_cast<const int *>(d_order);
+  P.goff = static_cast<const int *>(d_gate_off);
+  P.gks = static_cast<const int *>(d_gate_ks);
+  P.moff = static_cast<const int *>(d_meas_off);
+  P.mks = static_cast<const int *>(d_meas_ks);
+  P.gates = static_cast<const double *>(d_gates);
+  P.us = static_cast<const double *>(d_us);
+  P.outc = static_cast<int *>(d_outcomes);
+  P.probs = static_cast<double *>(d_probs);
+  P.ents = static_cast<double *>(d_entropy);
+  return launch_step(b, nt, P);
+}
+
+int tn_batch_stats(tn_batch *b, double *out, int32_t reset) {
+  if (!b) return TN_ERR_INVALID_ARG;
+  std::vector<double> v(size_t(STAT_N) * b->ntraj);
+  CKB(cudaMemcpyAsync(v.data(), b->dstats, sizeof(double) * v.size(), cudaMemcpyDeviceToHost, b->st));
+  if (reset) CKB(cudaMemsetAsync(b->dstats, 0, sizeof(double) * v.size(), b->st));
+  CKB(cudaStreamSynchronize(b->st));
+  if (out) {
+    for (int j = 0; j < STAT_N; ++j) out[j] = 0.0;
+    for (uint32_t t = 0; t < b->ntraj; ++t)
+      for (int j = 0; j < STAT_N; ++j) out[j] += v[size_t(t) * STAT_N + j];
+  }
   return TN_OK;
 }
 

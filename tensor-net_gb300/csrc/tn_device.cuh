@@ -460,7 +460,7 @@ __device__ void apply_right_block(cpx<T> *__restrict__ X, int ld, int rows, cons
 // Diagonalise the Hermitian W x W Gram matrix in sm.G by `nsweep` cyclic
 // sweeps with round-robin ordering; J accumulates the rotations (starts at I).
 template <typename T, int NT, int W>
-__device__ void jacobi_gram(Smem<T, W> &sm, int wcnt, T tol, int nsweep) {
+__device__ void jacobi_gram(Smem<T, W> &sm, int wcnt, T tol, T tiny2, int nsweep) {
   constexpr int H = W / 2;
   for (int idx = threadIdx.x; idx < W * W; idx += NT) {
     int p = idx / W, q = idx % W;
@@ -479,7 +479,7 @@ __device__ void jacobi_gram(Smem<T, W> &sm, int wcnt, T tol, int nsweep) {
           T a = sm.G[p * W + p].x, b = sm.G[q * W + q].x;
           cpx<T> g = sm.G[p * W + q];
           T ag = sqrt(cabs2(g));
-          if (a > T(0) && b > T(0) && ag > tol * sqrt(a) * sqrt(b)) {
+          if (a > tiny2 && b > tiny2 && ag > tol * sqrt(a) * sqrt(b)) {
             T zeta = (b - a) / (T(2) * ag);
             T t_ = T(1) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
             if (zeta < T(0)) t_ = -t_;
@@ -535,6 +535,16 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, cpx<T> *__restrict__ V, int el
                           Smem<T, W> &sm) {
   constexpr int B = W / 2;
   const T tol = sqrt(T(ell)) * Eps<T>::v;
+  // Columns with |a|^2 <= eps^2 ||A||_F^2 are rounding noise: rotating them
+  // changes nothing above rounding and their relative off-diagonals never
+  // settle, so they are neither rotated nor counted for convergence.
+  double fro = 0.0;
+  for (size_t idx = threadIdx.x; idx < size_t(ell) * c; idx += NT) {
+    cpx<T> x = A[idx];
+    fro += double(x.x) * x.x + double(x.y) * x.y;
+  }
+  fro = block_sum<NT>(fro, sm.red);
+  const T tiny2 = T(fro * double(Eps<T>::v) * double(Eps<T>::v));
   // V = I
   for (size_t idx = threadIdx.x; idx < size_t(c) * c; idx += NT) {
     int j = int(idx / c), i = int(idx % c);
@@ -574,13 +584,13 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, cpx<T> *__restrict__ V, int el
         if (p < q && q < wcnt) {
           T a = sm.G[p * W + p].x, b = sm.G[q * W + q].x;
           T ag = sqrt(cabs2(sm.G[idx]));
-          if (a > T(0) && b > T(0) && ag > tol * sqrt(a) * sqrt(b)) need = 1;
+          if (a > tiny2 && b > tiny2 && ag > tol * sqrt(a) * sqrt(b)) need = 1;
         }
       }
       need = __syncthreads_or(need);
       if (need) {
         rotated = 1;
-        jacobi_gram<T, NT, W>(sm, wcnt, tol, 1);
+        jacobi_gram<T, NT, W>(sm, wcnt, tol, tiny2, 1);
         apply_right_block<T, NT, W>(A, ell, ell, cols, wcnt, sm);
         apply_right_block<T, NT, W>(V, c, c, cols, wcnt, sm);
       }
@@ -664,10 +674,13 @@ __device__ void finalize_bond(const TrajDev &tr, int k, cpx<T> *__restrict__ gk,
   // rank rule on s/||s||
   int mode = tr.trunc_mode;
   double eps = (mode == 2 || mode == 3) ? fabs(tr.cutoff) : 2.220446049250313e-16;
-  // float32 theta carries ~sqrt(ell)*eps32 relative rounding: exact zeros of
-  // the spectrum come out at that level, so the MIXED path never keeps values
-  // below it (the float64 path keeps the reference's threshold unchanged).
-  if (sizeof(T) == 4) eps = fmax(eps, 2.0 * sqrt(double(ell)) * 1.1920928955078125e-07);
+  // Exact zeros of the spectrum come out of the Jacobi sweeps at about
+  // sqrt(ell)*eps_T relative to s_max (rounding of theta and of the
+  // rotations).  Values below that floor are noise in any SVD (LAPACK's
+  // included) and dividing by them (Gamma = U / Lambda) amplifies rounding,
+  // so they are never kept.  The floor only matters for None/Const (the
+  // reference's threshold is f64::EPSILON there); cutoffs >= 1e-12 are above it.
+  eps = fmax(eps, (sizeof(T) == 4 ? 2.0 : 4.0) * sqrt(double(ell)) * double(Eps<T>::v));
   int firstbad = c;
   for (int j = threadIdx.x; j < c; j += NT) {
     double s = key[j] / norm1;
@@ -778,7 +791,20 @@ __device__ void bond_op(const TrajDev &tr, int k, const double *gate, Work<T> &w
   double *lamM = lam_slot(tr, k + 1);
   build_theta<T, NT, W>(gk, gk1, lamL, lamM, lamR, cL, cM, cR, gate, wk.A, colmode, sm);
   int sw = jacobi_svd<T, NT, W>(wk.A, wk.V, ell, c, max_sweeps, sm);
-  if (sw < 0 && threadIdx.x == 0) atomicOr(tr.status, ST_NOT_CONVERGED);
+  if (threadIdx.x == 0) {
+    if (sw < 0) atomicOr(tr.status, ST_NOT_CONVERGED);
+    if (tr.stats) {
+      const double a = double(ell), b = double(c);
+      double ft = 8.0 * m * double(cM) * nc + (gate ? 128.0 * cL * cR : 0.0);
+      atomicAdd(tr.stats + STAT_FLOP_THETA, ft);
+      atomicAdd(tr.stats + STAT_FLOP_SVD, 4.0 * (4.0 * a * a * b + 8.0 * a * b * b + 9.0 * b * b * b));
+      atomicAdd(tr.stats + STAT_BOND_OPS, 1.0);
+      atomicAdd(tr.stats + STAT_SWEEPS, double(sw < 0 ? max_sweeps : sw));
+      // read the Gamma pair + Lambdas, write the new Gamma pair
+      const double eb = double(sizeof(cpx<T>));
+      atomicAdd(tr.stats + STAT_BYTES, eb * (2.0 * cL * cM + 2.0 * cM * cR) * 2.0 + 8.0 * (cL + cM + cR));
+    }
+  }
   finalize_bond<T, NT, W>(tr, k, gk, gk1, lamL, lamM, lamR, cL, cR, colmode, ell, c, wk, sm);
 }
 
@@ -815,6 +841,10 @@ __device__ void measure_site(const TrajDev &tr, int k, double u, int post, int *
   const double prob = outcome ? p1 : p0;
   const double sum = p0 + p1;
   if (threadIdx.x == 0) {
+    if (tr.stats) {
+      atomicAdd(tr.stats + STAT_MEAS, 1.0);
+      atomicAdd(tr.stats + STAT_BYTES, double(sizeof(cpx<T>)) * 2.0 * 2.0 * tr.chi[k] * tr.chi[k + 1]);
+    }
     if (out_outcome) *out_outcome = outcome;
     if (out_prob) *out_prob = prob;
     const double ptol = (sizeof(T) == 8) ? 1e-9 : 1e-4;

@@ -167,7 +167,7 @@ struct tn_mps {
   bool has_trunc = false;
   tn_trunc trunc{};
   cudaStream_t st = nullptr;
-  DevBuf gamma, lam, chi, status, dtraj;
+  DevBuf gamma, lam, chi, status, dtraj, stats;
   TrajDev h{};
   Launcher L;
 };
@@ -225,7 +225,10 @@ int mps_alloc(tn_mps *m) {
   CK(m->chi.ensure(sizeof(int) * (m->n + 1)));
   CK(m->status.ensure(sizeof(int)));
   CK(m->dtraj.ensure(sizeof(TrajDev)));
+  CK(m->stats.ensure(sizeof(double) * STAT_N));
+  CK(cudaMemsetAsync(m->stats.p, 0, sizeof(double) * STAT_N, m->st));
   TrajDev &d = m->h;
+  d.stats = m->stats.as<double>();
   d.gamma = m->gamma.p;
   d.lam = m->lam.as<double>();
   d.chi = m->chi.as<int>();
@@ -394,6 +397,7 @@ int tn_mps_free(tn_mps *m) {
   m->chi.release();
   m->status.release();
   m->dtraj.release();
+  m->stats.release();
   m->L.release();
   if (m->st) cudaStreamDestroy(m->st);
   delete m;
@@ -700,6 +704,14 @@ int tn_mps_contract(const tn_mps *m, double *out, uint64_t cap) {
     rows *= 2;
   }
   std::memcpy(out, psi.data(), sizeof(double) * 2 * dim);
+  return TN_OK;
+}
+
+int tn_mps_stats(tn_mps *m, double *out, int32_t reset) {
+  if (!m) return TN_ERR_INVALID_ARG;
+  if (out) CK(cudaMemcpyAsync(out, m->stats.p, sizeof(double) * STAT_N, cudaMemcpyDeviceToHost, m->st));
+  if (reset) CK(cudaMemsetAsync(m->stats.p, 0, sizeof(double) * STAT_N, m->st));
+  CK(cudaStreamSynchronize(m->st));
   return TN_OK;
 }
 

@@ -35,11 +35,23 @@ enum : int {
   ST_BAD_INSTR = 8,
 };
 
+// Per-trajectory counters accumulated by the kernels (float64 slots).
+enum : int {
+  STAT_FLOP_THETA = 0,  // 8*(2chiL)*chiM*(2chiR) (+128*chiL*chiR for a gate)
+  STAT_FLOP_SVD = 1,    // 4*(4a^2 b + 8ab^2 + 9b^3), a/b = max/min(2chiL, 2chiR)
+  STAT_BOND_OPS = 2,
+  STAT_SWEEPS = 3,
+  STAT_MEAS = 4,
+  STAT_BYTES = 5,       // algorithmic HBM bytes of the bond ops and measurements
+  STAT_N = 8
+};
+
 struct TrajDev {
   void *gamma;     // n slots of 2*cap*cap complex<T>
   double *lam;     // n+1 slots of cap float64
   int *chi;        // n+1 bond dimensions (chi[0] = chi[n] = 1)
   int *status;     // error word
+  double *stats;   // STAT_N counters
   int n, cap;
   int trunc_mode, chi_max;
   double cutoff;

@@ -236,6 +236,13 @@ class MPS:
         L.check(self._lib.tn_mps_contract(self._h, L.dptr(out), out.size), "contract")
         return out.view(np.complex128)
 
+    def stats(self, reset: bool = False):
+        """Device work counters: theta flops, SVD flops, bond ops, Jacobi
+        sweeps, measurements, algorithmic bytes."""
+        out = np.zeros(8)
+        L.check(self._lib.tn_mps_stats(self._h, L.dptr(out), int(reset)), "stats")
+        return dict(flop_theta=out[0], flop_svd=out[1], bond_ops=out[2], sweeps=out[3], meas=out[4], bytes=out[5])
+
     def device_status(self) -> int:
         st = L.i32()
         L.check(self._lib.tn_mps_device_status(self._h, C.byref(st)), "device_status")
