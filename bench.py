@@ -401,7 +401,7 @@ def main():
         "data": "synthetic (seeded Haar gates and measurement uniforms)",
         "config": dict(config, batch_per_gpu=r["B"], gpu=r["gpu"]),
         "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
-        "gpu_launches": 2 * a.steps,
+        "gpu_launches": 3 * a.steps,
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "peak_kind": f"{peaks_kind} bf16 sustained",
                      "traffic": (tr["bytes_per_launch_scale"] * r["stats"]["bytes"] / a.steps) if tr else None,

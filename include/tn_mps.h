@@ -164,11 +164,13 @@ int tn_mps_contract(const tn_mps *m, double *out, uint64_t cap);
 /* Device-side error word accumulated by this handle's kernels (0 if none);
  * cleared on read. */
 int tn_mps_device_status(tn_mps *m, int32_t *status);
-/* Work counters accumulated on the device since the last reset, 8 doubles:
+/* Work counters accumulated on the device since the last reset, 16 doubles:
  * [0] theta flops 8*(2chiL)*chiM*(2chiR) (+128*chiL*chiR per gate),
  * [1] SVD flops 4*(4a^2b + 8ab^2 + 9b^3) (a, b = larger/smaller side of theta),
  * [2] bond operations, [3] Jacobi sweeps, [4] measurements,
- * [5] algorithmic HBM bytes, [6..7] reserved.  reset != 0 zeroes them. */
+ * [5] algorithmic HBM bytes, [6..10] SM cycles spent in theta build, block
+ * Gram, block rotations, block update and finalisation, [11] Jacobi block
+ * steps, [12] refactors done through the LQ-reduced matrix, [13..15] reserved.  reset != 0 zeroes them. */
 int tn_mps_stats(tn_mps *m, double *out, int32_t reset);
 
 /* ==================== batch of trajectories (batching) ==================== */

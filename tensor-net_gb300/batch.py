@@ -109,9 +109,11 @@ class Batch:
         return int(st.value)
 
     def stats(self, reset: bool = False):
-        out = np.zeros(8)
+        out = np.zeros(16)
         L.check(self._lib.tn_batch_stats(self._h, L.dptr(out), int(reset)), "stats")
-        return dict(flop_theta=out[0], flop_svd=out[1], bond_ops=out[2], sweeps=out[3], meas=out[4], bytes=out[5])
+        return dict(flop_theta=out[0], flop_svd=out[1], bond_ops=out[2], sweeps=out[3], meas=out[4], bytes=out[5],
+                    cyc_theta=out[6], cyc_gram=out[7], cyc_rot=out[8], cyc_update=out[9], cyc_final=out[10],
+                    block_steps=out[11], lq_ops=out[12])
 
     def step_ptrs(self, nt, trajs, order, gate_off, gate_ks, gates, meas_off, meas_ks, us, outcomes, probs, entropy):
         """Layer step from device pointers (ints: int32, reals: float64)."""

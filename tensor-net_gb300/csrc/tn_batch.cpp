@@ -66,7 +66,11 @@ struct tn_batch {
   uint32_t step_nt = 0, step_ng = 0, step_nm = 0;
   Instr *dprog = nullptr;
   Item *ditems = nullptr;
-  int *dcounter = nullptr;
+  Instr *dgprog = nullptr;  // one single-gate program per gate of the layer
+  Item *dgitems = nullptr;
+  int gcap = 0;
+  uint32_t sum_n = 0;
+  int *dcounter = nullptr;  // [0] gate-launch queue, [1] reset list, [2] sweep-launch queue, [3] gate count
   // device-input mode
   void *din = nullptr;
   uint32_t din_gates = 0, din_meas = 0;
@@ -118,9 +122,14 @@ int ensure_step(tn_batch *b, uint32_t nt, uint32_t ng, uint32_t nm) {
   b->dprog = nullptr;
   CKB(cudaMalloc(&b->dstep, L.total));
   CKB(cudaMallocHost(&b->hstep, L.total));
-  CKB(cudaMalloc(reinterpret_cast<void **>(&b->dprog),
-                 sizeof(Instr) * size_t(NT) * b->pcap + sizeof(Item) * NT + 256));
-  b->ditems = reinterpret_cast<Item *>(reinterpret_cast<char *>(b->dprog) + sizeof(Instr) * size_t(NT) * b->pcap);
+  b->gcap = int(std::max<uint32_t>(NG, b->sum_n));
+  const size_t pbytes = sizeof(Instr) * size_t(NT) * b->pcap, ibytes = sizeof(Item) * NT;
+  const size_t gpbytes = sizeof(Instr) * size_t(b->gcap), gibytes = sizeof(Item) * size_t(b->gcap);
+  CKB(cudaMalloc(reinterpret_cast<void **>(&b->dprog), pbytes + ibytes + gpbytes + gibytes + 1024));
+  char *base = reinterpret_cast<char *>(b->dprog);
+  b->ditems = reinterpret_cast<Item *>(base + align256(pbytes));
+  b->dgprog = reinterpret_cast<Instr *>(base + align256(pbytes) + align256(ibytes));
+  b->dgitems = reinterpret_cast<Item *>(base + align256(pbytes) + align256(ibytes) + align256(gpbytes));
   b->step_nt = NT;
   b->step_ng = NG;
   b->step_nm = NM;
@@ -153,14 +162,11 @@ StepPtrs ptrs_of(const StepLayout &L, char *dbase) {
 
 int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P) {
   CKB(launch_compile(b->dtraj, P.list, int(nt), P.order, P.goff, P.gks, P.moff, P.mks, b->pcap, b->dprog, b->ditems,
-                     b->st));
-  CKB(cudaMemsetAsync(b->dcounter, 0, sizeof(int), b->st));
+                     b->dgprog, b->dgitems, b->gcap, b->dcounter + 3, b->st));
+  CKB(cudaMemsetAsync(b->dcounter, 0, 3 * sizeof(int), b->st));
   LaunchArgs la{};
-  la.items = b->ditems;
-  la.nitems = int(nt);
   la.counter = b->dcounter;
   la.trajs = b->dtraj;
-  la.prog = b->dprog;
   la.gates = P.gates;
   la.us = P.us;
   la.outcomes = P.outc;
@@ -170,6 +176,18 @@ int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P) {
   la.ws = b->ws;
   la.ws_stride = b->ws_stride;
   la.max_sweeps = 40;
+  // launch 1: every gate of the layer is an independent item
+  la.items = b->dgitems;
+  la.prog = b->dgprog;
+  la.nitems = 0;
+  la.nitems_dev = b->dcounter + 3;
+  CKB(launch_run(b->prec, la, b->grid_max, b->sortP, b->maxcap, b->st));
+  // launch 2: one measurement-layer program per trajectory
+  la.items = b->ditems;
+  la.prog = b->dprog;
+  la.nitems = int(nt);
+  la.nitems_dev = nullptr;
+  la.counter = b->dcounter + 2;
   const int grid = std::min<int>(int(nt), b->grid_max);
   CKB(launch_run(b->prec, la, grid, b->sortP, b->maxcap, b->st));
   return TN_OK;
@@ -216,6 +234,7 @@ int tn_batch_create(uint32_t ntraj, const uint32_t *ns, const tn_trunc *truncs, 
     total += bytes;
     b->maxcap = std::max<int>(b->maxcap, int(c));
     b->maxn = std::max<int>(b->maxn, int(ns[i]));
+    b->sum_n += ns[i];
   }
   auto bail = [&](int s) {
     tn_batch_free(b);
@@ -226,7 +245,7 @@ int tn_batch_create(uint32_t ntraj, const uint32_t *ns, const tn_trunc *truncs, 
   e = cudaMalloc(&b->arena, std::max<size_t>(total, 256));
   if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(arena)"));
   e = cudaMalloc(reinterpret_cast<void **>(&b->dtraj), sizeof(TrajDev) * ntraj + sizeof(double) * STAT_N * ntraj +
-                                                        sizeof(int) * (ntraj + 2));
+                                                        sizeof(int) * (ntraj + 8));
   if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(traj)"));
   b->dstats = reinterpret_cast<double *>(b->dtraj + ntraj);
   b->dstatus = reinterpret_cast<int *>(b->dstats + STAT_N * ntraj);
@@ -253,7 +272,7 @@ int tn_batch_create(uint32_t ntraj, const uint32_t *ns, const tn_trunc *truncs, 
     }
   }
   e = cudaMemcpyAsync(b->dtraj, b->h.data(), sizeof(TrajDev) * ntraj, cudaMemcpyHostToDevice, b->st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b->dstatus, 0, sizeof(int) * (ntraj + 2), b->st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->dstatus, 0, sizeof(int) * (ntraj + 8), b->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(b->dstats, 0, sizeof(double) * STAT_N * ntraj, b->st);
   if (e != cudaSuccess) return bail(fail(e, "init"));
   int dev = 0;
@@ -262,7 +281,7 @@ int tn_batch_create(uint32_t ntraj, const uint32_t *ns, const tn_trunc *truncs, 
   b->sortP = next_pow2(2 * b->maxcap);
   b->bps = run_blocks_per_sm(precision, b->sortP);
   b->grid_max = std::max(1, b->sms * b->bps);
-  b->grid_max = std::min<int>(b->grid_max, int(ntraj));
+  b->grid_max = std::min<int>(b->grid_max, int(std::max<uint32_t>(ntraj, b->sum_n / 2)));
   b->ws_stride = run_work_bytes(precision, b->maxcap);
   e = cudaMalloc(&b->ws, b->ws_stride * b->grid_max);
   if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(workspace)"));

@@ -156,59 +156,72 @@ __device__ __forceinline__ int block_min_int(int v, int *red) {
 }
 
 // ------------------------------------------------------- shared layout
-// W = columns per Jacobi block pair (two blocks of W/2).  TU = inner-dim
-// chunk of the theta build.
+// W = vectors per Jacobi block pair (two blocks of W/2).  The float path keeps
+// the block pair resident in shared memory when vectors have at most
+// RES_ROWS elements; otherwise (and for float64) it is streamed from L2 in
+// 32-row chunks.
 template <typename T, int W>
 struct SmemLayout {
   static constexpr int TU = 16;
   static constexpr int TILE = 32;                 // theta tile: 32 (v) x 32 (w)
-  static constexpr int TP = W + 1;                // padded row pitch of Ts
-  // region 0: theta tiles or sort keys (double) + perm (int)
-  static constexpr size_t gemm_bytes = size_t(2) * TILE * 2 * TU * sizeof(cpx<T>);
+  static constexpr int TP = W + 1;                // padded row pitch of Ts / Ab
+  static constexpr int RES_ROWS = sizeof(T) == 4 ? 512 : 0;
+  static constexpr int GK = 16, GT = 64;          // recovery GEMM: K chunk, 64x64 tile
+  static constexpr size_t theta_bytes = size_t(2) * TILE * 2 * TU * sizeof(cpx<T>);
+  static constexpr size_t gemm_bytes = size_t(2) * GK * (GT + 1) * sizeof(cpx<T>);
   __host__ __device__ static size_t sort_bytes(int P) { return size_t(P) * (sizeof(double) + sizeof(int)); }
   __host__ __device__ static size_t region0(int P) {
-    size_t g = gemm_bytes, s = sort_bytes(P);
+    size_t g = theta_bytes > gemm_bytes ? theta_bytes : gemm_bytes, s = sort_bytes(P);
     size_t r = g > s ? g : s;
     return (r + 255) & ~size_t(255);
   }
+  static constexpr size_t ab_bytes = size_t(RES_ROWS) * TP * sizeof(cpx<T>);
   static constexpr size_t g_bytes = size_t(W) * W * sizeof(cpx<T>);
   static constexpr size_t ts_bytes = size_t(32) * TP * sizeof(cpx<T>);
-  static constexpr size_t rot_bytes = size_t(W / 2) * (2 * sizeof(T) + sizeof(cpx<T>) + sizeof(int)) + 64;
-  static constexpr size_t red_bytes = 128 * sizeof(double);
+  static constexpr size_t rot_bytes = size_t(W) * (2 * sizeof(cpx<T>) + 2 * sizeof(int));
   __host__ __device__ static size_t total(int P) {
-    return region0(P) + 2 * g_bytes + ts_bytes + rot_bytes + red_bytes + 128 * sizeof(int) + 256;
+    return region0(P) + ab_bytes + 4 * g_bytes + ts_bytes + rot_bytes + 128 * sizeof(double) + 256 * sizeof(int) +
+           512;
   }
 };
 
 template <typename T, int W>
 struct Smem {
   unsigned char *r0;
-  cpx<T> *G, *J, *Ts;
-  T *rc, *rs;
-  cpx<T> *re;
-  int *rflag;
+  cpx<T> *Ab, *G, *G2, *J, *J2, *Ts;
+  cpx<T> *ca, *cb;  // per index i of a round: R[ra[i]][i], R[rb[i]][i]
+  int *ra, *rb;     // the rotation pair (p, q) containing i
   double *red;
   int *ired;
   __device__ Smem(unsigned char *base, int P) {
     using L = SmemLayout<T, W>;
+    auto al = [](unsigned char *q) {
+      return reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(q) + 15) & ~uintptr_t(15));
+    };
     unsigned char *p = base;
     r0 = p;
     p += L::region0(P);
+    Ab = reinterpret_cast<cpx<T> *>(p);
+    p += L::ab_bytes;
     G = reinterpret_cast<cpx<T> *>(p);
+    p += L::g_bytes;
+    G2 = reinterpret_cast<cpx<T> *>(p);
     p += L::g_bytes;
     J = reinterpret_cast<cpx<T> *>(p);
     p += L::g_bytes;
+    J2 = reinterpret_cast<cpx<T> *>(p);
+    p += L::g_bytes;
     Ts = reinterpret_cast<cpx<T> *>(p);
     p += L::ts_bytes;
-    re = reinterpret_cast<cpx<T> *>(p);
-    p += (W / 2) * sizeof(cpx<T>);
-    rc = reinterpret_cast<T *>(p);
-    p += (W / 2) * sizeof(T);
-    rs = reinterpret_cast<T *>(p);
-    p += (W / 2) * sizeof(T);
-    rflag = reinterpret_cast<int *>(p);
-    p += (W / 2) * sizeof(int) + 64 - ((W / 2) * sizeof(int)) % 64;
-    p = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15));
+    ca = reinterpret_cast<cpx<T> *>(p);
+    p += W * sizeof(cpx<T>);
+    cb = reinterpret_cast<cpx<T> *>(p);
+    p += W * sizeof(cpx<T>);
+    ra = reinterpret_cast<int *>(p);
+    p += W * sizeof(int);
+    rb = reinterpret_cast<int *>(p);
+    p += W * sizeof(int);
+    p = al(p);
     red = reinterpret_cast<double *>(p);
     p += 128 * sizeof(double);
     ired = reinterpret_cast<int *>(p);
@@ -216,19 +229,21 @@ struct Smem {
 };
 
 // ------------------------------------------------------------- workspace
+// Per-CTA global scratch (L2-resident for the CTA's current bond operation).
 template <typename T>
 struct Work {
   cpx<T> *A;     // Jacobi vectors, vector-contiguous, up to 4*cap^2
-  cpx<T> *V;     // accumulated rotations, up to 4*cap^2
-  T *scl;        // 2*cap row/column scale factors
+  cpx<T> *T0;    // copy of theta in the same layout (for the recovered side)
+  double *sig;   // 2*cap singular values, sorted descending
   double *s2;    // 2*cap kept Schmidt values
-  int *perm;     // 2*cap
+  T *scl;        // 2*cap row/column scale factors
+  int *perm;     // 2*cap source vector of each kept value
 };
 
 template <typename T>
 __host__ __device__ inline size_t work_bytes(int cap) {
   size_t n4 = size_t(4) * cap * cap;
-  size_t b = 2 * n4 * sizeof(cpx<T>) + size_t(2) * cap * sizeof(T) + size_t(2) * cap * sizeof(double) +
+  size_t b = 2 * n4 * sizeof(cpx<T>) + size_t(4) * cap * sizeof(double) + size_t(2) * cap * sizeof(T) +
              size_t(2) * cap * sizeof(int);
   return (b + 255) & ~size_t(255);
 }
@@ -240,8 +255,10 @@ __device__ inline Work<T> make_work(void *base, int cap) {
   size_t n4 = size_t(4) * cap * cap;
   w.A = reinterpret_cast<cpx<T> *>(p);
   p += n4 * sizeof(cpx<T>);
-  w.V = reinterpret_cast<cpx<T> *>(p);
+  w.T0 = reinterpret_cast<cpx<T> *>(p);
   p += n4 * sizeof(cpx<T>);
+  w.sig = reinterpret_cast<double *>(p);
+  p += size_t(2) * cap * sizeof(double);
   w.s2 = reinterpret_cast<double *>(p);
   p += size_t(2) * cap * sizeof(double);
   w.scl = reinterpret_cast<T *>(p);
@@ -268,15 +285,15 @@ __device__ __forceinline__ void rr_pair(int r, int t, int &p, int &q) {
 // Phase 1: theta = Lambda_{k-1} Gamma_k Lambda_k Gamma_{k+1} Lambda_{k+1},
 // then op on the fused physical pair (do_contract2 mps.rs:628-651,
 // contract_local2 732-754, apply_unitary2 1343-1352).
-// Writes A vector-contiguous: colmode A[j*m + i] = theta[i][j] (vectors =
-// columns, m >= nc), else A[i*nc + j] = theta[i][j] (vectors = rows).
+// Writes A (and its copy T0) vector-contiguous: colmode A[j*m + i] =
+// theta[i][j] (vectors = columns, m > nc), else A[i*nc + j] = theta[i][j].
 // =======================================================================
 template <typename T, int NT, int W>
 __device__ void build_theta(const cpx<T> *__restrict__ gk, const cpx<T> *__restrict__ gk1,
                             const double *__restrict__ lamL, const double *__restrict__ lamM,
                             const double *__restrict__ lamR, int cL, int cM, int cR,
-                            const double *__restrict__ gate, cpx<T> *__restrict__ A, bool colmode,
-                            Smem<T, W> &sm) {
+                            const double *__restrict__ gate, cpx<T> *__restrict__ A, cpx<T> *__restrict__ T0,
+                            bool colmode, Smem<T, W> &sm) {
   using L = SmemLayout<T, W>;
   constexpr int TILE = L::TILE, TU = L::TU;
   constexpr int PER = (TILE * TILE) / NT;  // (v,w) outputs per thread
@@ -357,10 +374,9 @@ __device__ void build_theta(const cpx<T> *__restrict__ gk, const cpx<T> *__restr
           for (int a = 0; a < 4; ++a) {
             int s1 = a >> 1, s2 = a & 1;
             int i = 2 * v + s1, j = s2 * cR + w;
-            if (colmode)
-              A[size_t(j) * ell + i] = th[a];
-            else
-              A[size_t(i) * ell + j] = th[a];
+            size_t o2 = colmode ? size_t(j) * ell + i : size_t(i) * ell + j;
+            A[o2] = th[a];
+            T0[o2] = th[a];
           }
         }
       }
@@ -371,13 +387,16 @@ __device__ void build_theta(const cpx<T> *__restrict__ gk, const cpx<T> *__restr
 
 // =======================================================================
 // Phase 2: one-sided (Hestenes) block Jacobi on the c vectors of length ell
-// stored in A; V (c x c, vector-contiguous) accumulates the right rotation.
-// Block pairs of W vectors: Gram G = Ab^H Ab (W x W), one cyclic sweep of
-// two-sided Jacobi on G with parallel (round-robin) ordering accumulating J,
-// then Ab <- Ab J and Vb <- Vb J.  Converged when every pair satisfies
-// |a_p^H a_q| <= tol * |a_p| |a_q| with tol = sqrt(ell) * eps.
-// Returns the number of outer sweeps, or -1 if the sweep limit was hit.
+// stored in A (vector-contiguous).  Block pairs of W vectors: Gram matrix
+// G = Ab^H Ab (W x W), one cyclic sweep of two-sided Jacobi on G with the
+// round-robin parallel ordering, accumulating J, then Ab <- Ab J.  Converged
+// when every pair satisfies |a_p^H a_q| <= tol |a_p| |a_q|, tol = sqrt(ell) eps.
+// The rotations are not accumulated: the other singular side is recovered
+// from the saved theta in the finalisation.  Returns the number of sweeps,
+// or -1 when the sweep limit was hit.
 // =======================================================================
+
+// -- streamed path (float64, or float with ell > RES_ROWS) ---------------
 template <typename T, int NT, int W>
 __device__ void load_block_chunk(const cpx<T> *__restrict__ A, int ell, const int *cols, int wcnt, int i0,
                                  cpx<T> *Ts) {
@@ -391,7 +410,7 @@ __device__ void load_block_chunk(const cpx<T> *__restrict__ A, int ell, const in
 }
 
 template <typename T, int NT, int W>
-__device__ void gram_block(const cpx<T> *__restrict__ A, int ell, const int *cols, int wcnt, Smem<T, W> &sm) {
+__device__ void gram_stream(const cpx<T> *__restrict__ A, int ell, const int *cols, int wcnt, Smem<T, W> &sm) {
   constexpr int TP = W + 1;
   constexpr int PER = (W * W + NT - 1) / NT;
   cpx<T> acc[PER];
@@ -421,10 +440,10 @@ __device__ void gram_block(const cpx<T> *__restrict__ A, int ell, const int *col
   __syncthreads();
 }
 
-// X (rows x W slice of a vector-contiguous matrix with vector length ld) <- X J
+// X (rows x W slice of a vector-contiguous matrix, vector length ld) <- X J
 template <typename T, int NT, int W>
-__device__ void apply_right_block(cpx<T> *__restrict__ X, int ld, int rows, const int *cols, int wcnt,
-                                  Smem<T, W> &sm) {
+__device__ void update_stream(cpx<T> *__restrict__ X, int ld, int rows, const int *cols, int wcnt,
+                              const cpx<T> *__restrict__ Jm, Smem<T, W> &sm) {
   constexpr int TP = W + 1;
   constexpr int PER = (32 * W + NT - 1) / NT;
   for (int i0 = 0; i0 < rows; i0 += 32) {
@@ -440,7 +459,7 @@ __device__ void apply_right_block(cpx<T> *__restrict__ X, int ld, int rows, cons
         int q = o >> 5, r = o & 31;
         if (q < wcnt) {
           cpx<T> a = czero<T>();
-          for (int p = 0; p < wcnt; ++p) a = cfma(sm.Ts[r * TP + p], sm.J[p * W + q], a);
+          for (int p = 0; p < wcnt; ++p) a = cfma(sm.Ts[r * TP + p], Jm[p * W + q], a);
           out[e] = a;
         }
       }
@@ -457,84 +476,184 @@ __device__ void apply_right_block(cpx<T> *__restrict__ X, int ld, int rows, cons
   __syncthreads();
 }
 
-// Diagonalise the Hermitian W x W Gram matrix in sm.G by `nsweep` cyclic
-// sweeps with round-robin ordering; J accumulates the rotations (starts at I).
+// -- resident path (float, ell <= RES_ROWS, W == 32) ---------------------
+// Ab[r][p] = A[cols[p]][r]; eight independent loads in flight per thread.
 template <typename T, int NT, int W>
-__device__ void jacobi_gram(Smem<T, W> &sm, int wcnt, T tol, T tiny2, int nsweep) {
-  constexpr int H = W / 2;
-  for (int idx = threadIdx.x; idx < W * W; idx += NT) {
-    int p = idx / W, q = idx % W;
-    sm.J[idx] = (p == q) ? mkc<T>(T(1), T(0)) : czero<T>();
-  }
-  __syncthreads();
-  for (int sw = 0; sw < nsweep; ++sw) {
-    for (int r = 0; r < W - 1; ++r) {
-      if (threadIdx.x < H) {
-        int t = threadIdx.x, p, q;
-        rr_pair<W>(r, t, p, q);
-        int flag = 0;
-        T c = T(1), s = T(0);
-        cpx<T> e = mkc<T>(T(1), T(0));
-        if (q < wcnt) {
-          T a = sm.G[p * W + p].x, b = sm.G[q * W + q].x;
-          cpx<T> g = sm.G[p * W + q];
-          T ag = sqrt(cabs2(g));
-          if (a > tiny2 && b > tiny2 && ag > tol * sqrt(a) * sqrt(b)) {
-            T zeta = (b - a) / (T(2) * ag);
-            T t_ = T(1) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-            if (zeta < T(0)) t_ = -t_;
-            c = T(1) / sqrt(T(1) + t_ * t_);
-            s = t_ * c;
-            e = mkc<T>(g.x / ag, -g.y / ag);  // e^{-i phi}, g = |g| e^{i phi}
-            flag = 1;
-          }
-        }
-        sm.rc[t] = c;
-        sm.rs[t] = s;
-        sm.re[t] = e;
-        sm.rflag[t] = flag;
-      }
-      __syncthreads();
-      // rows: G[p][j] <- c G[p][j] - s conj(e) G[q][j];  G[q][j] <- s G[p][j] + c conj(e) G[q][j]
-      for (int idx = threadIdx.x; idx < H * W; idx += NT) {
-        int t = idx / W, j = idx % W;
-        if (!sm.rflag[t]) continue;
-        int p, q;
-        rr_pair<W>(r, t, p, q);
-        T c = sm.rc[t], s = sm.rs[t];
-        cpx<T> ec = mkc<T>(sm.re[t].x, -sm.re[t].y);
-        cpx<T> gp = sm.G[p * W + j], gq = sm.G[q * W + j];
-        cpx<T> eq = cmul(ec, gq);
-        sm.G[p * W + j] = mkc<T>(c * gp.x - s * eq.x, c * gp.y - s * eq.y);
-        sm.G[q * W + j] = mkc<T>(s * gp.x + c * eq.x, s * gp.y + c * eq.y);
-      }
-      __syncthreads();
-      // columns of G and J: X[j][p] <- c X[j][p] - s e X[j][q];  X[j][q] <- s X[j][p] + c e X[j][q]
-      for (int idx = threadIdx.x; idx < 2 * H * W; idx += NT) {
-        int which = idx / (H * W);
-        int rem = idx % (H * W);
-        int t = rem / W, j = rem % W;
-        if (!sm.rflag[t]) continue;
-        int p, q;
-        rr_pair<W>(r, t, p, q);
-        T c = sm.rc[t], s = sm.rs[t];
-        cpx<T> e = sm.re[t];
-        cpx<T> *X = which ? sm.J : sm.G;
-        cpx<T> xp = X[j * W + p], xq = X[j * W + q];
-        cpx<T> eq = cmul(e, xq);
-        X[j * W + p] = mkc<T>(c * xp.x - s * eq.x, c * xp.y - s * eq.y);
-        X[j * W + q] = mkc<T>(s * xp.x + c * eq.x, s * xp.y + c * eq.y);
-      }
-      __syncthreads();
+__device__ void load_block_res(const cpx<T> *__restrict__ A, int ell, const int *cols, int wcnt, Smem<T, W> &sm) {
+  constexpr int TP = W + 1, UN = 8;
+  const int tot = W * ell;
+  for (int base = threadIdx.x; base < tot; base += NT * UN) {
+    cpx<T> v[UN];
+#pragma unroll
+    for (int u = 0; u < UN; ++u) {
+      const int idx = base + u * NT;
+      const int p = idx / ell, r = idx - p * ell;
+      v[u] = (idx < tot && p < wcnt) ? A[size_t(cols[p]) * ell + r] : czero<T>();
+    }
+#pragma unroll
+    for (int u = 0; u < UN; ++u) {
+      const int idx = base + u * NT;
+      const int p = idx / ell, r = idx - p * ell;
+      if (idx < tot) sm.Ab[r * TP + p] = v[u];
     }
   }
+  __syncthreads();
+}
+
+// G = Ab^H Ab: warp w owns rows 2w, 2w+1 of G, lane q its column; full sums
+// over ell (no cross-warp reduction).
+template <typename T, int NT, int W>
+__device__ void gram_res(int ell, Smem<T, W> &sm) {
+  static_assert(W == 32 && NT == 512, "resident Gram assumes W = 32, 16 warps");
+  constexpr int TP = W + 1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int p0 = 2 * warp;
+  cpx<T> a0 = czero<T>(), a1 = czero<T>(), b0 = czero<T>(), b1 = czero<T>();
+  int r = 0;
+  for (; r + 1 < ell; r += 2) {
+    const cpx<T> *row = sm.Ab + r * TP;
+    cpx<T> x0 = row[p0], x1 = row[p0 + 1], y = row[lane];
+    cpx<T> u0 = row[TP + p0], u1 = row[TP + p0 + 1], z = row[TP + lane];
+    a0 = cjfma(x0, y, a0);
+    a1 = cjfma(x1, y, a1);
+    b0 = cjfma(u0, z, b0);
+    b1 = cjfma(u1, z, b1);
+  }
+  if (r < ell) {
+    const cpx<T> *row = sm.Ab + r * TP;
+    cpx<T> x0 = row[p0], x1 = row[p0 + 1], y = row[lane];
+    a0 = cjfma(x0, y, a0);
+    a1 = cjfma(x1, y, a1);
+  }
+  sm.G[p0 * W + lane] = cadd(a0, b0);
+  sm.G[(p0 + 1) * W + lane] = cadd(a1, b1);
+  __syncthreads();
+}
+
+// A[:, cols] <- Ab J (Ab resident): thread owns 4 rows x 8 columns.
+template <typename T, int NT, int W>
+__device__ void update_res(cpx<T> *__restrict__ A, int ell, const int *cols, int wcnt,
+                           const cpx<T> *__restrict__ Jm, Smem<T, W> &sm) {
+  static_assert(W == 32 && NT % 4 == 0, "resident update layout");
+  constexpr int TP = W + 1, RB = NT / 4;
+  const int qb = threadIdx.x / RB, rb = threadIdx.x % RB;
+  const int q0 = qb * 8;
+  for (int r0 = 0; r0 < ell; r0 += 4 * RB) {
+    cpx<T> acc[4][8];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[i][j] = czero<T>();
+    for (int p = 0; p < wcnt; ++p) {
+      cpx<T> jr[8], a[4];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) jr[j] = Jm[p * W + q0 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        int r = r0 + rb + i * RB;
+        a[i] = r < ell ? sm.Ab[r * TP + p] : czero<T>();
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = cfma(a[i], jr[j], acc[i][j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      int r = r0 + rb + i * RB;
+      if (r < ell) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          if (q0 + j < wcnt) A[size_t(cols[q0 + j]) * ell + r] = acc[i][j];
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// One cyclic sweep of two-sided Jacobi on the Hermitian W x W matrix in
+// sm.G with round-robin ordering.  Each round computes its W/2 disjoint
+// rotations from the current G, then forms G' = R^H G R and J' = J R into
+// the other buffer (two barriers per round).  Returns the buffer holding J.
+template <typename T, int NT, int W>
+__device__ const cpx<T> *jacobi_gram(Smem<T, W> &sm, int wcnt, T tol, T tiny2) {
+  constexpr int H = W / 2;
+  cpx<T> *Gc = sm.G, *Gn = sm.G2, *Jc = sm.J, *Jn = sm.J2;
+  for (int idx = threadIdx.x; idx < W * W; idx += NT) {
+    int p = idx / W, q = idx % W;
+    Jc[idx] = (p == q) ? mkc<T>(T(1), T(0)) : czero<T>();
+  }
+  __syncthreads();
+  for (int r = 0; r < W - 1; ++r) {
+    if (threadIdx.x < H) {
+      int t = threadIdx.x, p, q;
+      rr_pair<W>(r, t, p, q);
+      T c = T(1), sn = T(0);
+      cpx<T> e = mkc<T>(T(1), T(0));
+      bool rot = false;
+      if (q < wcnt) {
+        T a = Gc[p * W + p].x, b = Gc[q * W + q].x;
+        cpx<T> g = Gc[p * W + q];
+        T ag = sqrt(cabs2(g));
+        if (a > tiny2 && b > tiny2 && ag > tol * sqrt(a) * sqrt(b)) {
+          T zeta = (b - a) / (T(2) * ag);
+          T t_ = T(1) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+          if (zeta < T(0)) t_ = -t_;
+          c = T(1) / sqrt(T(1) + t_ * t_);
+          sn = t_ * c;
+          e = mkc<T>(g.x / ag, -g.y / ag);  // e^{-i phi}, g = |g| e^{i phi}
+          rot = true;
+        }
+      }
+      // R on (p, q): column p = (c, -s e), column q = (s, c e); identity if no rotation
+      sm.ra[p] = p;
+      sm.rb[p] = q;
+      sm.ra[q] = p;
+      sm.rb[q] = q;
+      sm.ca[p] = rot ? mkc<T>(c, T(0)) : mkc<T>(T(1), T(0));
+      sm.cb[p] = rot ? cscale(e, -sn) : czero<T>();
+      sm.ca[q] = rot ? mkc<T>(sn, T(0)) : czero<T>();
+      sm.cb[q] = rot ? cscale(e, c) : mkc<T>(T(1), T(0));
+    }
+    __syncthreads();
+    // G'[i][j] = sum_{a in pair(i)} conj(R[a][i]) sum_{b in pair(j)} G[a][b] R[b][j];  J' = J R
+    for (int idx = threadIdx.x; idx < 2 * W * W; idx += NT) {
+      const bool isJ = idx >= W * W;
+      const int o = isJ ? idx - W * W : idx;
+      const int i = o / W, j = o % W;
+      const int jp = sm.ra[j], jq = sm.rb[j];
+      const cpx<T> rjp = sm.ca[j], rjq = sm.cb[j];
+      if (isJ) {
+        Jn[o] = cfma(Jc[i * W + jq], rjq, cmul(Jc[i * W + jp], rjp));
+      } else {
+        const int ip = sm.ra[i], iq = sm.rb[i];
+        const cpx<T> rip = sm.ca[i], riq = sm.cb[i];
+        cpx<T> gpj = cfma(Gc[ip * W + jq], rjq, cmul(Gc[ip * W + jp], rjp));
+        cpx<T> gqj = cfma(Gc[iq * W + jq], rjq, cmul(Gc[iq * W + jp], rjp));
+        Gn[o] = cjfma(riq, gqj, cmul(mkc<T>(rip.x, -rip.y), gpj));
+      }
+    }
+    __syncthreads();
+    cpx<T> *t1 = Gc;
+    Gc = Gn;
+    Gn = t1;
+    t1 = Jc;
+    Jc = Jn;
+    Jn = t1;
+  }
+  return Jc;
 }
 
 template <typename T, int NT, int W>
-__device__ int jacobi_svd(cpx<T> *__restrict__ A, cpx<T> *__restrict__ V, int ell, int c, int max_sweeps,
-                          Smem<T, W> &sm) {
+__device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps, Smem<T, W> &sm,
+                          long long *cyc) {
+  using L = SmemLayout<T, W>;
   constexpr int B = W / 2;
-  const T tol = sqrt(T(ell)) * Eps<T>::v;
+  const bool resident = (L::RES_ROWS > 0) && ell <= L::RES_ROWS;
+  // Rounding noise of a computed Gram entry is about sqrt(ell) eps |a_p||a_q|;
+  // the threshold sits a factor 4 above it so that converged pairs are not
+  // rotated again on noise alone.
+  const T tol = T(4) * sqrt(T(ell)) * Eps<T>::v;
   // Columns with |a|^2 <= eps^2 ||A||_F^2 are rounding noise: rotating them
   // changes nothing above rounding and their relative off-diagonals never
   // settle, so they are neither rotated nor counted for convergence.
@@ -545,14 +664,8 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, cpx<T> *__restrict__ V, int el
   }
   fro = block_sum<NT>(fro, sm.red);
   const T tiny2 = T(fro * double(Eps<T>::v) * double(Eps<T>::v));
-  // V = I
-  for (size_t idx = threadIdx.x; idx < size_t(c) * c; idx += NT) {
-    int j = int(idx / c), i = int(idx % c);
-    V[idx] = (i == j) ? mkc<T>(T(1), T(0)) : czero<T>();
-  }
-  __syncthreads();
   const int nblk = (c + B - 1) / B;
-  int *cols = sm.ired + 64;  // W ints (ired[0..64) is reduction scratch)
+  int *cols = sm.ired + 128;  // W ints (ired[0..128) is reduction scratch)
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     int rotated = 0;
     const int npairs = (nblk <= 2) ? 1 : nblk * (nblk - 1) / 2;
@@ -576,8 +689,17 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, cpx<T> *__restrict__ V, int el
         cols[t] = col;
       }
       __syncthreads();
-      gram_block<T, NT, W>(A, ell, cols, wcnt, sm);
-      // off-diagonal test
+      long long t0 = clock64();
+      if constexpr (L::RES_ROWS > 0) {
+        if (resident) {
+          load_block_res<T, NT, W>(A, ell, cols, wcnt, sm);
+          gram_res<T, NT, W>(ell, sm);
+        } else {
+          gram_stream<T, NT, W>(A, ell, cols, wcnt, sm);
+        }
+      } else {
+        gram_stream<T, NT, W>(A, ell, cols, wcnt, sm);
+      }
       int need = 0;
       for (int idx = threadIdx.x; idx < W * W; idx += NT) {
         int p = idx / W, q = idx % W;
@@ -588,13 +710,25 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, cpx<T> *__restrict__ V, int el
         }
       }
       need = __syncthreads_or(need);
+      long long t1 = clock64();
+      cyc[0] += t1 - t0;
+      cyc[3] += 1;
       if (need) {
         rotated = 1;
-        jacobi_gram<T, NT, W>(sm, wcnt, tol, tiny2, 1);
-        apply_right_block<T, NT, W>(A, ell, ell, cols, wcnt, sm);
-        apply_right_block<T, NT, W>(V, c, c, cols, wcnt, sm);
+        const cpx<T> *Jm = jacobi_gram<T, NT, W>(sm, wcnt, tol, tiny2);
+        long long t2 = clock64();
+        cyc[1] += t2 - t1;
+        t1 = t2;
+        if constexpr (L::RES_ROWS > 0) {
+          if (resident)
+            update_res<T, NT, W>(A, ell, cols, wcnt, Jm, sm);
+          else
+            update_stream<T, NT, W>(A, ell, ell, cols, wcnt, Jm, sm);
+        } else {
+          update_stream<T, NT, W>(A, ell, ell, cols, wcnt, Jm, sm);
+        }
+        cyc[2] += clock64() - t1;
       }
-      // next block pair (row-cyclic)
       if (++Jb >= nblk) {
         ++I;
         Jb = I + 1;
@@ -635,6 +769,56 @@ __device__ void bitonic_desc(double *key, int *idx, int P) {
   }
 }
 
+// C[x][y] = sum_k P(x,k) Q(y,k) over 64x64 output tiles (8 per thread),
+// K staged through shared memory in chunks of 16; E(x, y, value) stores.
+template <typename T, int NT, int W, class FP, class FQ, class FE>
+__device__ void gemm_nt(int M, int N, int K, FP P, FQ Q, FE E, Smem<T, W> &sm) {
+  using L = SmemLayout<T, W>;
+  constexpr int GK = L::GK, GT = L::GT, PITCH = GT + 1;
+  static_assert(NT == 512, "gemm_nt thread layout");
+  cpx<T> *Ps = reinterpret_cast<cpx<T> *>(sm.r0);  // [GK][GT+1]
+  cpx<T> *Qs = Ps + GK * PITCH;                    // [GK][GT+1]
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;  // 16 x 32
+  for (int x0 = 0; x0 < M; x0 += GT) {
+    for (int y0 = 0; y0 < N; y0 += GT) {
+      cpx<T> acc[4][2];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc[i][0] = acc[i][1] = czero<T>();
+      for (int k0 = 0; k0 < K; k0 += GK) {
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < GK * GT; idx += NT) {
+          int kk = idx % GK, xx = idx / GK;
+          int gx = x0 + xx, gk = k0 + kk;
+          Ps[kk * PITCH + xx] = (gx < M && gk < K) ? P(gx, gk) : czero<T>();
+          int gy = y0 + xx;
+          Qs[kk * PITCH + xx] = (gy < N && gk < K) ? Q(gy, gk) : czero<T>();
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < GK; ++kk) {
+          cpx<T> pv[4], qv[2];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) pv[i] = Ps[kk * PITCH + tx * 4 + i];
+#pragma unroll
+          for (int j = 0; j < 2; ++j) qv[j] = Qs[kk * PITCH + ty * 2 + j];
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) acc[i][j] = cfma(pv[i], qv[j], acc[i][j]);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          int x = x0 + tx * 4 + i, y = y0 + ty * 2 + j;
+          if (x < M && y < N) E(x, y, acc[i][j]);
+        }
+    }
+  }
+  __syncthreads();
+}
+
 template <typename T, int NT, int W>
 __device__ void finalize_bond(const TrajDev &tr, int k, cpx<T> *__restrict__ gk, cpx<T> *__restrict__ gk1,
                               const double *__restrict__ lamL, double *__restrict__ lamM,
@@ -648,7 +832,7 @@ __device__ void finalize_bond(const TrajDev &tr, int k, cpx<T> *__restrict__ gk,
   double *key = reinterpret_cast<double *>(sm.r0);
   int *pidx = reinterpret_cast<int *>(key + P);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  // column norms (float64 accumulation)
+  // vector norms (float64 accumulation)
   for (int j = warp; j < P; j += NT / 32) {
     double acc = 0.0;
     if (j < c) {
@@ -706,10 +890,10 @@ __device__ void finalize_bond(const TrajDev &tr, int k, cpx<T> *__restrict__ gk,
     part2 += s * s;
   }
   const double norm2 = sqrt(block_sum<NT>(part2, sm.red));
-  // kept values s2 = (s/norm1)/norm2; scale factors for the rebuild
   for (int j = threadIdx.x; j < rank; j += NT) {
     double s1 = key[j] / norm1;
     wk.s2[j] = s1 / norm2;
+    wk.sig[j] = key[j];
     wk.perm[j] = pidx[j];
   }
   // scl[0..cL): 1/Lambda_{k-1}[v]; scl[cap..cap+cR): norm2/Lambda_{k+1}[w]
@@ -718,34 +902,42 @@ __device__ void finalize_bond(const TrajDev &tr, int k, cpx<T> *__restrict__ gk,
   for (int w = threadIdx.x; w < cR; w += NT) sclR[w] = T(norm2 / lamR[w]);
   __syncthreads();
   const int m = 2 * cL, nc = 2 * cR;
-  // Gamma_k[v,s1,j] = U[(v s1), j] / Lambda_{k-1}[v]
-  for (size_t idx = threadIdx.x; idx < size_t(m) * rank; idx += NT) {
-    int i = int(idx / rank), j = int(idx % rank);
-    int src = wk.perm[j];
-    cpx<T> u;
-    if (colmode) {
-      T inv = T(1.0 / key[j]);  // U[:, j] = A_src / sigma_src
-      u = cscale(wk.A[size_t(src) * ell + i], inv);
-    } else {
-      cpx<T> vv = wk.V[size_t(src) * c + i];
-      u = mkc<T>(vv.x, -vv.y);
+  const cpx<T> *A = wk.A, *T0 = wk.T0;
+  const double *sig = wk.sig;
+  const int *perm = wk.perm;
+  if (colmode) {
+    // vectors = columns: U[:, j] = a_src / sigma (direct)
+    for (size_t idx = threadIdx.x; idx < size_t(m) * rank; idx += NT) {
+      int i = int(idx / rank), j = int(idx % rank);
+      gk[idx] = cscale(A[size_t(perm[j]) * ell + i], T(1.0 / sig[j]) * sclL[i >> 1]);
     }
-    gk[idx] = cscale(u, sclL[i >> 1]);
-  }
-  // Gamma_{k+1}[j, s2, w] = Vh[j, (s2 w)] * norm2 / Lambda_{k+1}[w]
-  for (size_t idx = threadIdx.x; idx < size_t(rank) * nc; idx += NT) {
-    int j = int(idx / nc), col = int(idx % nc);
-    int src = wk.perm[j];
-    cpx<T> vh;
-    if (colmode) {
-      cpx<T> vv = wk.V[size_t(src) * c + col];
-      vh = mkc<T>(vv.x, -vv.y);
-    } else {
-      T inv = T(1.0 / key[j]);  // Vh[j, :] = A_src / sigma_src
-      vh = cscale(wk.A[size_t(src) * ell + col], inv);
+    // Vh[j][col] = sum_i conj(a_src[i]) theta[i][col] / sigma^2 (recovered)
+    gemm_nt<T, NT, W>(
+        rank, nc, m,
+        [&](int j, int i) {
+          cpx<T> a = A[size_t(perm[j]) * ell + i];
+          return mkc<T>(a.x, -a.y);
+        },
+        [&](int col, int i) { return T0[size_t(col) * m + i]; },
+        [&](int j, int col, cpx<T> v) {
+          gk1[size_t(j) * nc + col] = cscale(v, T(1.0 / (sig[j] * sig[j])) * sclR[col % cR]);
+        },
+        sm);
+  } else {
+    // vectors = rows: Vh[j, :] = w_src / sigma (direct)
+    for (size_t idx = threadIdx.x; idx < size_t(rank) * nc; idx += NT) {
+      int j = int(idx / nc), col = int(idx % nc);
+      gk1[idx] = cscale(A[size_t(perm[j]) * ell + col], T(1.0 / sig[j]) * sclR[col % cR]);
     }
-    int w = col % cR;
-    gk1[idx] = cscale(vh, sclR[w]);
+    // U[i][j] = sum_col theta[i][col] conj(w_src[col]) / sigma^2 (recovered)
+    gemm_nt<T, NT, W>(
+        m, rank, nc, [&](int i, int col) { return T0[size_t(i) * nc + col]; },
+        [&](int j, int col) {
+          cpx<T> a = A[size_t(perm[j]) * ell + col];
+          return mkc<T>(a.x, -a.y);
+        },
+        [&](int i, int j, cpx<T> v) { gk[size_t(i) * rank + j] = cscale(v, T(1.0 / (sig[j] * sig[j])) * sclL[i >> 1]); },
+        sm);
   }
   __syncthreads();
   // local_renormalize(k) and (k+1) with the new Lambda_k = s2
@@ -778,23 +970,115 @@ __device__ __forceinline__ cpx<T> *gamma_slot(const TrajDev &tr, int k) {
 }
 __device__ __forceinline__ double *lam_slot(const TrajDev &tr, int s) { return tr.lam + size_t(s) * tr.cap; }
 
+// In-place Cholesky S = L L^H of the n x n Hermitian matrix S (row-major,
+// global scratch; the lower triangle becomes L).  Fails (returns false) when
+// a pivot falls below `rel` times the original diagonal entry, i.e. when the
+// rows behind S are far from orthonormal.
+template <typename T, int NT, int W>
+__device__ bool cholesky_lower(cpx<T> *__restrict__ S, int n, double rel, double *__restrict__ diag0,
+                               Smem<T, W> &sm) {
+  for (int i = threadIdx.x; i < n; i += NT) diag0[i] = double(S[size_t(i) * n + i].x);
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    const double d = double(S[size_t(k) * n + k].x);
+    if (!(d > rel * diag0[k]) || !(d > 0.0)) return false;  // uniform: every thread read the same value
+    const T l = T(sqrt(d)), il = T(1.0 / sqrt(d));
+    __syncthreads();
+    for (int i = k + 1 + threadIdx.x; i < n; i += NT) S[size_t(i) * n + k] = cscale(S[size_t(i) * n + k], il);
+    if (threadIdx.x == 0) S[size_t(k) * n + k] = mkc<T>(l, T(0));
+    __syncthreads();
+    const int rem = n - k - 1;
+    for (int idx = threadIdx.x; idx < rem * rem; idx += NT) {
+      const int i = k + 1 + idx / rem, j = k + 1 + idx % rem;
+      if (j > i) continue;
+      const cpx<T> li = S[size_t(i) * n + k], lj = S[size_t(j) * n + k];
+      // S[i][j] -= L[i][k] conj(L[j][k])
+      cpx<T> v = S[size_t(i) * n + j];
+      v.x -= li.x * lj.x + li.y * lj.y;
+      v.y -= li.y * lj.x - li.x * lj.y;
+      S[size_t(i) * n + j] = v;
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
+// Refactor through the LQ factor of the right block (local_refactor,
+// mps.rs:846-880).  theta = X diag(Lambda_k) B with X = Lambda_{k-1} Gamma_k
+// (m x chiM) and B = Gamma_{k+1} Lambda_{k+1} (chiM x nc).  With
+// B B^H = L L^H, Q = L^{-1} B has orthonormal rows and theta = M Q,
+// M = X diag(Lambda_k) L: the singular values and left vectors of theta are
+// those of M (chiM columns), and Vh = U^H theta / sigma is recovered from
+// theta itself.  In (near-)canonical form L is close to the identity, M has
+// nearly orthogonal columns and the Jacobi sweeps converge in two or three
+// passes.  Returns false (and leaves theta in wk.T0 untouched) when B is too
+// far from orthonormal rows for the factorisation to be accurate.
+template <typename T, int NT, int W>
+__device__ bool refactor_lq(const cpx<T> *__restrict__ gk, const cpx<T> *__restrict__ gk1,
+                            const double *__restrict__ lamL, const double *__restrict__ lamM,
+                            const double *__restrict__ lamR, int cL, int cM, int cR, int cap, Work<T> &wk,
+                            Smem<T, W> &sm) {
+  const int m = 2 * cL, nc = 2 * cR;
+  cpx<T> *S = wk.A + size_t(2) * cap * cap;  // chiM x chiM, after M's m x chiM region
+  // S = B B^H
+  gemm_nt<T, NT, W>(
+      cM, cM, nc, [&](int x, int col) { return cscale(gk1[size_t(x) * nc + col], T(lamR[col % cR])); },
+      [&](int y, int col) {
+        cpx<T> b = cscale(gk1[size_t(y) * nc + col], T(lamR[col % cR]));
+        return mkc<T>(b.x, -b.y);
+      },
+      [&](int x, int y, cpx<T> v) { S[size_t(x) * cM + y] = v; }, sm);
+  const double rel = sizeof(T) == 4 ? 0.1 : 1e-3;
+  if (!cholesky_lower<T, NT, W>(S, cM, rel, wk.sig, sm)) return false;
+  // M = X diag(Lambda_k) L, stored vector-contiguous: A[j*m + i] = M[i][j]
+  cpx<T> *A = wk.A;
+  gemm_nt<T, NT, W>(
+      m, cM, cM,
+      [&](int i, int u) { return cscale(gk[size_t(i) * cM + u], T(lamL[i >> 1] * lamM[u])); },
+      [&](int j, int u) { return u >= j ? S[size_t(u) * cM + j] : czero<T>(); },
+      [&](int i, int j, cpx<T> v) { A[size_t(j) * m + i] = v; }, sm);
+  return true;
+}
+
 // One bond operation on (k, k+1): gate != nullptr -> apply_unitary2, else local_refactor.
 template <typename T, int NT, int W>
 __device__ void bond_op(const TrajDev &tr, int k, const double *gate, Work<T> &wk, int max_sweeps,
                         Smem<T, W> &sm) {
   const int cL = tr.chi[k], cM = tr.chi[k + 1], cR = tr.chi[k + 2];
   const int m = 2 * cL, nc = 2 * cR;
-  const bool colmode = m > nc;  // square: vectors = rows (coalesced theta stores)
-  const int ell = colmode ? m : nc, c = colmode ? nc : m;
   cpx<T> *gk = gamma_slot<T>(tr, k), *gk1 = gamma_slot<T>(tr, k + 1);
   const double *lamL = lam_slot(tr, k), *lamR = lam_slot(tr, k + 2);
   double *lamM = lam_slot(tr, k + 1);
-  build_theta<T, NT, W>(gk, gk1, lamL, lamM, lamR, cL, cM, cR, gate, wk.A, colmode, sm);
-  int sw = jacobi_svd<T, NT, W>(wk.A, wk.V, ell, c, max_sweeps, sm);
+  long long c0 = clock64();
+  // Refactors of a bond whose theta has more columns than its rank bound
+  // chiM go through the LQ-reduced matrix M (m x chiM); gates and small
+  // bonds take the direct path on theta.
+  bool lq = false;
+  if (!gate && cM < nc && cM <= m) {
+    build_theta<T, NT, W>(gk, gk1, lamL, lamM, lamR, cL, cM, cR, nullptr, wk.T0, wk.T0, true, sm);
+    lq = refactor_lq<T, NT, W>(gk, gk1, lamL, lamM, lamR, cL, cM, cR, tr.cap, wk, sm);
+  }
+  bool colmode;
+  int ell, c;
+  if (lq) {
+    colmode = true;
+    ell = m;
+    c = cM;
+  } else {
+    colmode = m > nc;  // square: vectors = rows (coalesced theta stores)
+    ell = colmode ? m : nc;
+    c = colmode ? nc : m;
+    build_theta<T, NT, W>(gk, gk1, lamL, lamM, lamR, cL, cM, cR, gate, wk.A, wk.T0, colmode, sm);
+  }
+  long long c1 = clock64();
+  long long cyc[4] = {0, 0, 0, 0};
+  int sw = jacobi_svd<T, NT, W>(wk.A, ell, c, max_sweeps, sm, cyc);
+  long long c2 = clock64();
   if (threadIdx.x == 0) {
     if (sw < 0) atomicOr(tr.status, ST_NOT_CONVERGED);
     if (tr.stats) {
-      const double a = double(ell), b = double(c);
+      if (lq) atomicAdd(tr.stats + STAT_LQ_OPS, 1.0);
+      const double a = double(m > nc ? m : nc), b = double(m > nc ? nc : m);
       double ft = 8.0 * m * double(cM) * nc + (gate ? 128.0 * cL * cR : 0.0);
       atomicAdd(tr.stats + STAT_FLOP_THETA, ft);
       atomicAdd(tr.stats + STAT_FLOP_SVD, 4.0 * (4.0 * a * a * b + 8.0 * a * b * b + 9.0 * b * b * b));
@@ -806,6 +1090,14 @@ __device__ void bond_op(const TrajDev &tr, int k, const double *gate, Work<T> &w
     }
   }
   finalize_bond<T, NT, W>(tr, k, gk, gk1, lamL, lamM, lamR, cL, cR, colmode, ell, c, wk, sm);
+  if (threadIdx.x == 0 && tr.stats) {
+    atomicAdd(tr.stats + STAT_CYC_THETA, double(c1 - c0));
+    atomicAdd(tr.stats + STAT_CYC_GRAM, double(cyc[0]));
+    atomicAdd(tr.stats + STAT_CYC_ROT, double(cyc[1]));
+    atomicAdd(tr.stats + STAT_CYC_UPDATE, double(cyc[2]));
+    atomicAdd(tr.stats + STAT_CYC_FINAL, double(clock64() - c2));
+    atomicAdd(tr.stats + STAT_BLOCK_STEPS, double(cyc[3]));
+  }
 }
 
 // local_probs (mps.rs:1079-1134): p_s = sum L_{k-1}[v]^2 |G[v,s,u]|^2 L_k[u]^2
@@ -935,6 +1227,8 @@ __device__ void run_program(const LaunchArgs &la, const Item &it, Work<T> &wk, S
         __syncthreads();
         break;
       }
+      case OP_NOP:
+        break;
       default:
         if (threadIdx.x == 0) atomicOr(tr.status, ST_BAD_INSTR);
         break;

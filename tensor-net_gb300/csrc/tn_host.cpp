@@ -142,9 +142,11 @@ void emit_sweep(std::vector<Instr> &prog, uint32_t n) {
 
 // Launch scratch shared by the single-state API calls of one handle.
 struct Launcher {
-  DevBuf prog, items, counter, gates, us, outc, probs, ents, pout, ws;
-  int sortP = 1, ws_cap = 1;
+  DevBuf prog, items, counter, gates, us, outc, probs, ents, pout, ws, gprog, gitems;
+  int sortP = 1, ws_cap = 1, ws_ctas = 1, sms = 1;
   void release() {
+    gprog.release();
+    gitems.release();
     prog.release();
     items.release();
     counter.release();
@@ -239,6 +241,11 @@ int mps_alloc(tn_mps *m) {
   CK(cudaMemcpyAsync(m->dtraj.p, &d, sizeof(TrajDev), cudaMemcpyHostToDevice, m->st));
   CK(cudaMemsetAsync(m->status.p, 0, sizeof(int), m->st));
   m->L.ws_cap = int(m->cap);
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&m->L.sms, cudaDevAttrMultiProcessorCount, dev);
+  }
   m->L.sortP = next_pow2(2 * int(m->cap));
   CK(m->L.ws.ensure(run_work_bytes(m->prec, m->L.ws_cap)));
   return TN_OK;
@@ -256,20 +263,55 @@ int mps_reset(tn_mps *m) {
 // synchronised) only when a pointer is given.
 int mps_run(tn_mps *m, const std::vector<Instr> &prog, const std::vector<double> &gates,
             const std::vector<double> &us, int n_meas_out, int32_t *outc, double *probs, int n_ent_out,
-            double *ents, int n_pout, double *pout) {
-  if (prog.empty()) return TN_OK;
+            double *ents, int n_pout, double *pout, const std::vector<Instr> &par = {}) {
+  if (prog.empty() && par.empty()) return TN_OK;
   Launcher &L = m->L;
+  if (!par.empty()) {
+    // independent single-operation items (disjoint gates) spread over SMs
+    const int np = int(par.size());
+    const int grid = std::max(1, std::min(np, L.sms));
+    if (grid > L.ws_ctas) {
+      CK(cudaStreamSynchronize(m->st));
+      L.ws.release();
+      CK(L.ws.ensure(run_work_bytes(m->prec, L.ws_cap) * size_t(grid)));
+      L.ws_ctas = grid;
+    }
+    std::vector<Item> it(np);
+    for (int i = 0; i < np; ++i) it[i] = Item{0, i, 1, 0};
+    CK(L.gprog.ensure(np * sizeof(Instr)));
+    CK(L.gitems.ensure(np * sizeof(Item)));
+    CK(L.counter.ensure(2 * sizeof(int)));
+    CK(L.gates.ensure(std::max<size_t>(1, gates.size()) * sizeof(double)));
+    CK(cudaMemcpyAsync(L.gprog.p, par.data(), np * sizeof(Instr), cudaMemcpyHostToDevice, m->st));
+    CK(cudaMemcpyAsync(L.gitems.p, it.data(), np * sizeof(Item), cudaMemcpyHostToDevice, m->st));
+    if (!gates.empty())
+      CK(cudaMemcpyAsync(L.gates.p, gates.data(), gates.size() * sizeof(double), cudaMemcpyHostToDevice, m->st));
+    CK(cudaMemsetAsync(L.counter.p, 0, 2 * sizeof(int), m->st));
+    LaunchArgs la{};
+    la.items = L.gitems.as<Item>();
+    la.nitems = np;
+    la.counter = L.counter.as<int>() + 1;
+    la.trajs = m->dtraj.as<TrajDev>();
+    la.prog = L.gprog.as<Instr>();
+    la.gates = L.gates.as<double>();
+    la.ws = L.ws.p;
+    la.ws_stride = run_work_bytes(m->prec, L.ws_cap);
+    la.max_sweeps = kMaxSweeps;
+    CK(launch_run(m->prec, la, grid, L.sortP, L.ws_cap, m->st));
+    if (prog.empty()) return TN_OK;
+  }
   CK(L.prog.ensure(prog.size() * sizeof(Instr)));
   CK(L.items.ensure(sizeof(Item)));
   CK(L.counter.ensure(sizeof(int)));
   CK(L.gates.ensure(std::max<size_t>(1, gates.size()) * sizeof(double)));
   CK(L.us.ensure(std::max<size_t>(1, us.size()) * sizeof(double)));
+  const bool gates_loaded = !par.empty();
   CK(L.outc.ensure(std::max(1, n_meas_out) * sizeof(int)));
   CK(L.probs.ensure(std::max(1, n_meas_out) * sizeof(double)));
   CK(L.ents.ensure(std::max(1, n_ent_out) * sizeof(double)));
   CK(L.pout.ensure(std::max(1, 2 * n_pout) * sizeof(double)));
   CK(cudaMemcpyAsync(L.prog.p, prog.data(), prog.size() * sizeof(Instr), cudaMemcpyHostToDevice, m->st));
-  if (!gates.empty())
+  if (!gates.empty() && !gates_loaded)
     CK(cudaMemcpyAsync(L.gates.p, gates.data(), gates.size() * sizeof(double), cudaMemcpyHostToDevice, m->st));
   if (!us.empty())
     CK(cudaMemcpyAsync(L.us.p, us.data(), us.size() * sizeof(double), cudaMemcpyHostToDevice, m->st));
@@ -577,12 +619,19 @@ int tn_mps_apply_bilayer(tn_mps *m, const uint32_t *gate_ks, const double *gates
                          const uint32_t *meas_ks, uint32_t nm, const double *us, uint32_t *out_ks,
                          int32_t *outcomes, double *probs, uint32_t *n_out) {
   if (!m || (ng && (!gate_ks || !gates)) || (nm && (!meas_ks || !us))) return TN_ERR_INVALID_ARG;
-  std::vector<Instr> prog;
+  std::vector<Instr> prog, par;
   std::vector<double> g;
   g.reserve(size_t(ng) * 32);
+  bool disjoint = true;
+  for (uint32_t i = 0; i < ng && disjoint; ++i)
+    for (uint32_t j = i + 1; j < ng; ++j)
+      if ((gate_ks[i] > gate_ks[j] ? gate_ks[i] - gate_ks[j] : gate_ks[j] - gate_ks[i]) < 2) {
+        disjoint = false;
+        break;
+      }
   for (uint32_t i = 0; i < ng; ++i) {
     if (m->n == 1 || gate_ks[i] >= m->n - 1) continue;
-    prog.push_back(Instr{OP_GATE, int(gate_ks[i]), int(g.size() / 32), 0});
+    (disjoint ? par : prog).push_back(Instr{OP_GATE, int(gate_ks[i]), int(g.size() / 32), 0});
     g.insert(g.end(), gates + size_t(i) * 32, gates + size_t(i + 1) * 32);
   }
   std::vector<uint32_t> tk;
@@ -594,7 +643,7 @@ int tn_mps_apply_bilayer(tn_mps *m, const uint32_t *gate_ks, const double *gates
   std::vector<int32_t> oc(std::max<size_t>(1, tk.size()));
   std::vector<double> pr(std::max<size_t>(1, tk.size()));
   int s = mps_run(m, prog, g, u, int(tk.size()), tk.empty() ? nullptr : oc.data(), tk.empty() ? nullptr : pr.data(),
-                  0, nullptr, 0, nullptr);
+                  0, nullptr, 0, nullptr, par);
   if (s != TN_OK) return s;
   for (size_t j = 0; j < tk.size(); ++j) {
     if (out_ks) out_ks[j] = tk[j];

@@ -43,7 +43,14 @@ enum : int {
   STAT_SWEEPS = 3,
   STAT_MEAS = 4,
   STAT_BYTES = 5,       // algorithmic HBM bytes of the bond ops and measurements
-  STAT_N = 8
+  STAT_CYC_THETA = 6,   // SM cycles (thread 0 clock64) per phase of the bond operations
+  STAT_CYC_GRAM = 7,
+  STAT_CYC_ROT = 8,     // inner Jacobi on the block Gram matrix
+  STAT_CYC_UPDATE = 9,
+  STAT_CYC_FINAL = 10,
+  STAT_BLOCK_STEPS = 11,
+  STAT_LQ_OPS = 12,     // refactors done through the LQ-reduced matrix
+  STAT_N = 16
 };
 
 struct TrajDev {
@@ -64,6 +71,7 @@ struct Item {
 struct LaunchArgs {
   const Item *items;
   int nitems;
+  const int *nitems_dev;  // when set, the item count is read from device memory
   int *counter;
   TrajDev *trajs;
   const Instr *prog;
@@ -85,7 +93,7 @@ int run_blocks_per_sm(int prec, int sortP);
 cudaError_t launch_reset(TrajDev *trajs, const int *list, int count, int prec, cudaStream_t st);
 cudaError_t launch_compile(const TrajDev *trajs, const int *list, int nt, const int *order, const int *gate_off,
                            const int *gate_ks, const int *meas_off, const int *meas_ks, int pcap, Instr *prog,
-                           Item *items, cudaStream_t st);
+                           Item *items, Instr *gprog, Item *gitems, int gcap, int *gcount, cudaStream_t st);
 
 inline int next_pow2(int x) {
   int p = 1;

@@ -24,7 +24,7 @@ __global__ void __launch_bounds__(NT, 1) k_run(LaunchArgs la, int sortP, int ws_
     __syncthreads();
     const int it = s_item;
     __syncthreads();
-    if (it >= la.nitems) break;
+    if (it >= (la.nitems_dev ? *la.nitems_dev : la.nitems)) break;
     run_program<T, NT, W>(la, la.items[it], wk, sm);
   }
 }
@@ -50,13 +50,19 @@ __global__ void k_reset(TrajDev *trajs, const int *list, int count, int elem_byt
   }
 }
 
-// One thread per listed trajectory.  Program of list entry i lives at
-// prog + i * pcap; items[order[i]] points at it so that the executor pulls
-// the most expensive trajectories first.
+// One thread per listed trajectory.  The layer's gates act on disjoint bonds
+// (a brickwork layer, circuit.rs:523-563), so each becomes its own work item
+// (gprog[g], gitems[g]) of the first launch, spread over all SMs; the
+// measurement layer with its refactor sweep and the entropy read form the
+// trajectory's program of the second launch, at prog + i * pcap, placed at
+// items[order[i]] so that the executor pulls the most expensive trajectories
+// first.  A trajectory whose gates overlap keeps them, in order, at the head
+// of its second-launch program instead.
 __global__ void k_compile(const TrajDev *trajs, const int *list, int nt, const int *order, const int *gate_off,
                           const int *gate_ks, const int *meas_off, const int *meas_ks, int pcap, Instr *prog,
-                          Item *items) {
+                          Item *items, Instr *gprog, Item *gitems, int gcap, int *gcount) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *gcount = min(gate_off[nt], gcap);
   if (i >= nt) return;
   const int t = list[i];
   const int n = trajs[t].n;
@@ -66,9 +72,24 @@ __global__ void k_compile(const TrajDev *trajs, const int *list, int nt, const i
     if (pc < pcap) p[pc] = Instr{op, k, a, b};
     ++pc;
   };
-  for (int g = gate_off[i]; g < gate_off[i + 1]; ++g) {
+  const int g0 = gate_off[i], g1 = gate_off[i + 1];
+  bool disjoint = true;
+  for (int g = g0; g < g1 && disjoint; ++g)
+    for (int h = g + 1; h < g1; ++h)
+      if (abs(gate_ks[g] - gate_ks[h]) < 2) {
+        disjoint = false;
+        break;
+      }
+  for (int g = g0; g < g1; ++g) {
     const int k = gate_ks[g];
-    if (n > 1 && k >= 0 && k < n - 1) emit(OP_GATE, k, g, 0);
+    const bool valid = n > 1 && k >= 0 && k < n - 1;
+    if (g < gcap) {
+      gprog[g] = (disjoint && valid) ? Instr{OP_GATE, k, g, 0} : Instr{OP_NOP, 0, 0, 0};
+      gitems[g] = Item{t, g, 1, 0};
+    } else if (disjoint) {
+      atomicOr(trajs[t].status, ST_BAD_INSTR);
+    }
+    if (!disjoint && valid) emit(OP_GATE, k, g, 0);
   }
   const int m0 = meas_off[i], m1 = meas_off[i + 1];
   int last = -1;
@@ -141,10 +162,10 @@ cudaError_t launch_reset(TrajDev *trajs, const int *list, int count, int prec, c
 
 cudaError_t launch_compile(const TrajDev *trajs, const int *list, int nt, const int *order, const int *gate_off,
                            const int *gate_ks, const int *meas_off, const int *meas_ks, int pcap, Instr *prog,
-                           Item *items, cudaStream_t st) {
+                           Item *items, Instr *gprog, Item *gitems, int gcap, int *gcount, cudaStream_t st) {
   if (nt <= 0) return cudaSuccess;
   k_compile<<<(nt + 127) / 128, 128, 0, st>>>(trajs, list, nt, order, gate_off, gate_ks, meas_off, meas_ks, pcap,
-                                              prog, items);
+                                              prog, items, gprog, gitems, gcap, gcount);
   return cudaGetLastError();
 }
 

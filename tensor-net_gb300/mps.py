@@ -239,9 +239,11 @@ class MPS:
     def stats(self, reset: bool = False):
         """Device work counters: theta flops, SVD flops, bond ops, Jacobi
         sweeps, measurements, algorithmic bytes."""
-        out = np.zeros(8)
+        out = np.zeros(16)
         L.check(self._lib.tn_mps_stats(self._h, L.dptr(out), int(reset)), "stats")
-        return dict(flop_theta=out[0], flop_svd=out[1], bond_ops=out[2], sweeps=out[3], meas=out[4], bytes=out[5])
+        return dict(flop_theta=out[0], flop_svd=out[1], bond_ops=out[2], sweeps=out[3], meas=out[4], bytes=out[5],
+                    cyc_theta=out[6], cyc_gram=out[7], cyc_rot=out[8], cyc_update=out[9], cyc_final=out[10],
+                    block_steps=out[11], lq_ops=out[12])
 
     def device_status(self) -> int:
         st = L.i32()
