@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--batch", type=int, default=0, help="trajectories per GPU (0: one per resident CTA)")
+    ap.add_argument("--batch", type=int, default=512, help="trajectories per GPU")
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--chi", type=int, default=256)
     ap.add_argument("--cutoff", type=float, default=1e-10)
@@ -248,7 +248,7 @@ def run_gpu(a, rank, world, local_rank):
     name = ctypes.create_string_buffer(128)
     sms = ctypes.c_uint32()
     pkg._lib.check(lib.tn_device_info(name, 128, ctypes.byref(sms)), "tn_device_info")
-    B = a.batch or int(sms.value)
+    B = a.batch
     n, chi = a.n, a.chi
     trunc = pkg.Trunc.both(chi, a.cutoff)
     batch = pkg.Batch([n] * B, [trunc] * B, a.prec)
@@ -301,11 +301,13 @@ def run_gpu(a, rank, world, local_rank):
     clocks = ClockSampler(local_rank)
     clocks.start()
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps + 1)]
+    split = []
     with torch.cuda.stream(stream):
         evs[0].record(stream)
         for i, s in enumerate(staged[a.warmup:]):
             launch(s)
             evs[i + 1].record(stream)
+            split.append(batch.last_launch_ms())
     batch.synchronize()
     torch.cuda.synchronize()
     clk = clocks.stop()
@@ -338,7 +340,7 @@ def run_gpu(a, rank, world, local_rank):
                                                                          2 * B + 2 * (B + 1))) for pk in packs)
     d2h = statistics.mean(int(int(pk["meas_off"][-1]) * (4 + 8) + 8 * B) for pk in packs)
     dims = [batch.bond_dims(i) for i in range(min(B, 5))]
-    return dict(value=value, elapsed=elapsed, step_ms=step_ms, stats=st, status=status, clocks=clk,
+    return dict(value=value, elapsed=elapsed, step_ms=step_ms, split=split, stats=st, status=status, clocks=clk,
                 e2e=world * B * a.steps / e2e_s, h2d=h2d, d2h=d2h, B=B, gpu=name.value.decode(),
                 ents=ents, dims=dims, sms=int(sms.value), layer_inputs=layer_inputs)
 
@@ -412,6 +414,8 @@ def main():
         "work": {"bond_ops_per_step": r["stats"]["bond_ops"] / a.steps,
                  "jacobi_sweeps_per_op": r["stats"]["sweeps"] / max(1.0, r["stats"]["bond_ops"]),
                  "meas_per_step": r["stats"]["meas"] / a.steps, "step_ms": r["step_ms"],
+                 "gate_launch_ms, sweep_launch_ms": r["split"],
+                 "lq_refactors_per_step": r["stats"]["lq_ops"] / a.steps,
                  "device_status": r["status"], "middle_bond_dims": [int(d[a.n // 2 - 1]) for d in r["dims"]]},
     }
     if rank == 0 and world == 1 and not a.no_cpu:

@@ -227,6 +227,15 @@ int tn_batch_device_status(tn_batch *b, int32_t *status);
 int tn_batch_stats(tn_batch *b, double *out, int32_t reset);
 /* Device bytes held by slot t (its footprint for admission control). */
 int tn_batch_slot_bytes(tn_batch *b, uint32_t t, uint64_t *bytes);
+/* Jacobi tuning of the batch (picked by the autotuner): scheme 0 visits all
+ * vector pairs of each block pair of a sweep, scheme 1 visits every pair once
+ * per sweep (within-block steps, then cross-block steps); max_sweeps bounds
+ * the sweeps of one SVD (1..200, default 40). */
+int tn_batch_set_tuning(tn_batch *b, int32_t scheme, int32_t max_sweeps);
+/* Device time of the last non-graph step, split into the gate launch (all
+ * gates of the layer as independent items) and the sweep launch (measurement
+ * layers, refactor sweeps, entropy reads).  TN_NONE before any such step. */
+int tn_batch_last_launch_ms(tn_batch *b, float *gate_ms, float *sweep_ms);
 /* Stream the batch launches on (a cudaStream_t), for callers that time with
  * CUDA events. */
 int tn_batch_stream(tn_batch *b, void **stream);

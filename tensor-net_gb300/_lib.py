@@ -72,6 +72,8 @@ SIGNATURES = {
     "tn_batch_device_status": (C.c_int, [vp, P(i32)]),
     "tn_batch_slot_bytes": (C.c_int, [vp, u32, P(u64)]),
     "tn_batch_stream": (C.c_int, [vp, P(vp)]),
+    "tn_batch_last_launch_ms": (C.c_int, [vp, P(C.c_float), P(C.c_float)]),
+    "tn_batch_set_tuning": (C.c_int, [vp, i32, i32]),
     "tn_haar_u4": (C.c_int, [P(dbl), P(dbl)]),
     "tn_gen_layer": (C.c_int, [u64, u64, u32, u32, dbl, P(u32), P(dbl), P(u32), P(u32), P(dbl), P(u32)]),
     "tn_gen_ginibre": (C.c_int, [u64, u64, u32, u32, P(dbl)]),

@@ -130,5 +130,14 @@ class Batch:
         L.check(self._lib.tn_batch_stream(self._h, C.byref(s)), "stream")
         return int(s.value or 0)
 
+    def set_tuning(self, scheme: int = 0, max_sweeps: int = 40):
+        L.check(self._lib.tn_batch_set_tuning(self._h, int(scheme), int(max_sweeps)), "set_tuning")
+
+    def last_launch_ms(self):
+        """(gate launch ms, sweep launch ms) of the last non-graph step."""
+        g, w = C.c_float(), C.c_float()
+        s = L.check(self._lib.tn_batch_last_launch_ms(self._h, C.byref(g), C.byref(w)), "last_launch_ms")
+        return None if s == L.TN_NONE else (g.value, w.value)
+
     def synchronize(self):
         L.check(self._lib.tn_batch_synchronize(self._h), "synchronize")

@@ -25,10 +25,8 @@ extern "C" const char *tn_last_error(void);
 
 namespace {
 
-thread_local std::string g_err;
-
 int fail(cudaError_t e, const char *what) {
-  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  tn::set_last_error(what, e);
   if (e == cudaErrorMemoryAllocation) return TN_ERR_OOM;
   return TN_ERR_CUDA;
 }
@@ -51,6 +49,7 @@ struct tn_batch {
   cudaStream_t st = nullptr;
   int sms = 1, bps = 1, grid_max = 1;
   int maxcap = 1, maxn = 1, sortP = 1, pcap = 8;
+  int scheme = 0, max_sweeps = 40;  // Jacobi tuning (tn_batch_set_tuning)
   std::vector<uint32_t> n_alloc, cap;
   std::vector<TrajDev> h;
   std::vector<size_t> slot_bytes;
@@ -75,6 +74,8 @@ struct tn_batch {
   void *din = nullptr;
   uint32_t din_gates = 0, din_meas = 0;
   std::map<uint32_t, cudaGraphExec_t> graphs;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // around the gate and sweep launches
+  bool ev_recorded = false;
 };
 
 namespace {
@@ -160,7 +161,7 @@ StepPtrs ptrs_of(const StepLayout &L, char *dbase) {
   return p;
 }
 
-int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P) {
+int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P, bool timed = true) {
   CKB(launch_compile(b->dtraj, P.list, int(nt), P.order, P.goff, P.gks, P.moff, P.mks, b->pcap, b->dprog, b->ditems,
                      b->dgprog, b->dgitems, b->gcap, b->dcounter + 3, b->st));
   CKB(cudaMemsetAsync(b->dcounter, 0, 3 * sizeof(int), b->st));
@@ -175,13 +176,16 @@ int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P) {
   la.pout = P.probs;
   la.ws = b->ws;
   la.ws_stride = b->ws_stride;
-  la.max_sweeps = 40;
+  la.max_sweeps = b->max_sweeps;
+  la.jacobi_scheme = b->scheme;
   // launch 1: every gate of the layer is an independent item
   la.items = b->dgitems;
   la.prog = b->dgprog;
   la.nitems = 0;
   la.nitems_dev = b->dcounter + 3;
+  if (timed) CKB(cudaEventRecord(b->ev[0], b->st));
   CKB(launch_run(b->prec, la, b->grid_max, b->sortP, b->maxcap, b->st));
+  if (timed) CKB(cudaEventRecord(b->ev[1], b->st));
   // launch 2: one measurement-layer program per trajectory
   la.items = b->ditems;
   la.prog = b->dprog;
@@ -190,6 +194,10 @@ int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P) {
   la.counter = b->dcounter + 2;
   const int grid = std::min<int>(int(nt), b->grid_max);
   CKB(launch_run(b->prec, la, grid, b->sortP, b->maxcap, b->st));
+  if (timed) {
+    CKB(cudaEventRecord(b->ev[2], b->st));
+    b->ev_recorded = true;
+  }
   return TN_OK;
 }
 
@@ -242,6 +250,10 @@ int tn_batch_create(uint32_t ntraj, const uint32_t *ns, const tn_trunc *truncs, 
   };
   cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
   if (e != cudaSuccess) return bail(fail(e, "cudaStreamCreate"));
+  for (auto &ev : b->ev) {
+    e = cudaEventCreate(&ev);
+    if (e != cudaSuccess) return bail(fail(e, "cudaEventCreate"));
+  }
   e = cudaMalloc(&b->arena, std::max<size_t>(total, 256));
   if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(arena)"));
   e = cudaMalloc(reinterpret_cast<void **>(&b->dtraj), sizeof(TrajDev) * ntraj + sizeof(double) * STAT_N * ntraj +
@@ -311,6 +323,8 @@ int tn_batch_free(tn_batch *b) {
   if (b->ws) cudaFree(b->ws);
   if (b->dtraj) cudaFree(b->dtraj);
   if (b->arena) cudaFree(b->arena);
+  for (auto &ev : b->ev)
+    if (ev) cudaEventDestroy(ev);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
   return TN_OK;
@@ -450,7 +464,7 @@ int tn_batch_step_device(tn_batch *b, uint32_t nt) {
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ge = nullptr;
     CKB(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
-    int s = launch_step(b, nt, ptrs_of(L, reinterpret_cast<char *>(b->din)));
+    int s = launch_step(b, nt, ptrs_of(L, reinterpret_cast<char *>(b->din)), false);
     cudaError_t e = cudaStreamEndCapture(b->st, &g);
     if (s != TN_OK) {
       if (g) cudaGraphDestroy(g);
@@ -550,6 +564,27 @@ int tn_batch_device_status(tn_batch *b, int32_t *status) {
 int tn_batch_slot_bytes(tn_batch *b, uint32_t t, uint64_t *bytes) {
   if (!b || t >= b->ntraj || !bytes) return TN_ERR_INVALID_ARG;
   *bytes = b->slot_bytes[t];
+  return TN_OK;
+}
+
+int tn_batch_set_tuning(tn_batch *b, int32_t scheme, int32_t max_sweeps) {
+  if (!b || scheme < 0 || scheme > 1 || max_sweeps < 1 || max_sweeps > 200) return TN_ERR_INVALID_ARG;
+  for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);  // captured launches carry the old values
+  b->graphs.clear();
+  b->scheme = scheme;
+  b->max_sweeps = max_sweeps;
+  return TN_OK;
+}
+
+int tn_batch_last_launch_ms(tn_batch *b, float *gate_ms, float *sweep_ms) {
+  if (!b) return TN_ERR_INVALID_ARG;
+  if (!b->ev_recorded) return TN_NONE;
+  CKB(cudaEventSynchronize(b->ev[2]));
+  float g = 0.f, w = 0.f;
+  CKB(cudaEventElapsedTime(&g, b->ev[0], b->ev[1]));
+  CKB(cudaEventElapsedTime(&w, b->ev[1], b->ev[2]));
+  if (gate_ms) *gate_ms = g;
+  if (sweep_ms) *sweep_ms = w;
   return TN_OK;
 }
 

@@ -238,13 +238,17 @@ struct Work {
   double *s2;    // 2*cap kept Schmidt values
   T *scl;        // 2*cap row/column scale factors
   int *perm;     // 2*cap source vector of each kept value
+  T *lam3;       // 3*cap: Lambda_{k-1}, Lambda_k, Lambda_{k+1} in the working precision
+  T *isig;       // 2*cap: 1/sigma_j and (after cap*2) 1/sigma_j^2 of the kept values
+  T *isig2;
+  T *w2;         // 2*cap: s2_j^2 in the working precision
 };
 
 template <typename T>
 __host__ __device__ inline size_t work_bytes(int cap) {
   size_t n4 = size_t(4) * cap * cap;
   size_t b = 2 * n4 * sizeof(cpx<T>) + size_t(4) * cap * sizeof(double) + size_t(2) * cap * sizeof(T) +
-             size_t(2) * cap * sizeof(int);
+             size_t(2) * cap * sizeof(int) + size_t(3) * cap * sizeof(T) + size_t(6) * cap * sizeof(T) + 256;
   return (b + 255) & ~size_t(255);
 }
 
@@ -264,6 +268,15 @@ __device__ inline Work<T> make_work(void *base, int cap) {
   w.scl = reinterpret_cast<T *>(p);
   p += size_t(2) * cap * sizeof(T);
   w.perm = reinterpret_cast<int *>(p);
+  p += size_t(2) * cap * sizeof(int);
+  p = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15));
+  w.lam3 = reinterpret_cast<T *>(p);
+  p += size_t(3) * cap * sizeof(T);
+  w.isig = reinterpret_cast<T *>(p);
+  p += size_t(2) * cap * sizeof(T);
+  w.isig2 = reinterpret_cast<T *>(p);
+  p += size_t(2) * cap * sizeof(T);
+  w.w2 = reinterpret_cast<T *>(p);
   return w;
 }
 
@@ -290,8 +303,8 @@ __device__ __forceinline__ void rr_pair(int r, int t, int &p, int &q) {
 // =======================================================================
 template <typename T, int NT, int W>
 __device__ void build_theta(const cpx<T> *__restrict__ gk, const cpx<T> *__restrict__ gk1,
-                            const double *__restrict__ lamL, const double *__restrict__ lamM,
-                            const double *__restrict__ lamR, int cL, int cM, int cR,
+                            const T *__restrict__ lamL, const T *__restrict__ lamM,
+                            const T *__restrict__ lamR, int cL, int cM, int cR,
                             const double *__restrict__ gate, cpx<T> *__restrict__ A, cpx<T> *__restrict__ T0,
                             bool colmode, Smem<T, W> &sm) {
   using L = SmemLayout<T, W>;
@@ -329,7 +342,7 @@ __device__ void build_theta(const cpx<T> *__restrict__ gk, const cpx<T> *__restr
           int w = idx % TILE, s = (idx / TILE) & 1, u = idx / (2 * TILE);
           int gw = w0 + w, gu = u0 + u;
           cpx<T> y = czero<T>();
-          if (gw < cR && gu < cM) y = cscale(gk1[(size_t(gu) * 2 + s) * cR + gw], T(lamM[gu]));
+          if (gw < cR && gu < cM) y = cscale(gk1[(size_t(gu) * 2 + s) * cR + gw], lamM[gu]);
           Ys[idx] = y;
         }
         __syncthreads();
@@ -354,7 +367,7 @@ __device__ void build_theta(const cpx<T> *__restrict__ gk, const cpx<T> *__restr
         int o = tid + e * NT;
         int v = v0 + o / TILE, w = w0 + o % TILE;
         if (v < cL && w < cR) {
-          T sl = T(lamL[v]), sr = T(lamR[w]);
+          const T sl = lamL[v], sr = lamR[w];
           cpx<T> th[4];
 #pragma unroll
           for (int q = 0; q < 4; ++q) th[q] = cscale(cscale(acc[e][q], sl), sr);
@@ -398,19 +411,18 @@ __device__ void build_theta(const cpx<T> *__restrict__ gk, const cpx<T> *__restr
 
 // -- streamed path (float64, or float with ell > RES_ROWS) ---------------
 template <typename T, int NT, int W>
-__device__ void load_block_chunk(const cpx<T> *__restrict__ A, int ell, const int *cols, int wcnt, int i0,
-                                 cpx<T> *Ts) {
+__device__ void load_block_chunk(const cpx<T> *__restrict__ A, int ell, const int *cols, int i0, cpx<T> *Ts) {
   constexpr int TP = W + 1;
   for (int idx = threadIdx.x; idx < 32 * W; idx += NT) {
     int r = idx & 31, p = idx >> 5;
     cpx<T> v = czero<T>();
-    if (p < wcnt && i0 + r < ell) v = A[size_t(cols[p]) * ell + i0 + r];
+    if (cols[p] >= 0 && i0 + r < ell) v = A[size_t(cols[p]) * ell + i0 + r];
     Ts[r * TP + p] = v;
   }
 }
 
 template <typename T, int NT, int W>
-__device__ void gram_stream(const cpx<T> *__restrict__ A, int ell, const int *cols, int wcnt, Smem<T, W> &sm) {
+__device__ void gram_stream(const cpx<T> *__restrict__ A, int ell, const int *cols, Smem<T, W> &sm) {
   constexpr int TP = W + 1;
   constexpr int PER = (W * W + NT - 1) / NT;
   cpx<T> acc[PER];
@@ -418,7 +430,7 @@ __device__ void gram_stream(const cpx<T> *__restrict__ A, int ell, const int *co
   for (int e = 0; e < PER; ++e) acc[e] = czero<T>();
   for (int i0 = 0; i0 < ell; i0 += 32) {
     __syncthreads();
-    load_block_chunk<T, NT, W>(A, ell, cols, wcnt, i0, sm.Ts);
+    load_block_chunk<T, NT, W>(A, ell, cols, i0, sm.Ts);
     __syncthreads();
     const int rmax = min(32, ell - i0);
 #pragma unroll
@@ -442,13 +454,13 @@ __device__ void gram_stream(const cpx<T> *__restrict__ A, int ell, const int *co
 
 // X (rows x W slice of a vector-contiguous matrix, vector length ld) <- X J
 template <typename T, int NT, int W>
-__device__ void update_stream(cpx<T> *__restrict__ X, int ld, int rows, const int *cols, int wcnt,
+__device__ void update_stream(cpx<T> *__restrict__ X, int ld, int rows, const int *cols,
                               const cpx<T> *__restrict__ Jm, Smem<T, W> &sm) {
   constexpr int TP = W + 1;
   constexpr int PER = (32 * W + NT - 1) / NT;
   for (int i0 = 0; i0 < rows; i0 += 32) {
     __syncthreads();
-    load_block_chunk<T, NT, W>(X, ld, cols, wcnt, i0, sm.Ts);
+    load_block_chunk<T, NT, W>(X, ld, cols, i0, sm.Ts);
     __syncthreads();
     cpx<T> out[PER];
 #pragma unroll
@@ -457,9 +469,9 @@ __device__ void update_stream(cpx<T> *__restrict__ X, int ld, int rows, const in
       out[e] = czero<T>();
       if (o < 32 * W) {
         int q = o >> 5, r = o & 31;
-        if (q < wcnt) {
+        if (cols[q] >= 0) {
           cpx<T> a = czero<T>();
-          for (int p = 0; p < wcnt; ++p) a = cfma(sm.Ts[r * TP + p], Jm[p * W + q], a);
+          for (int p = 0; p < W; ++p) a = cfma(sm.Ts[r * TP + p], Jm[p * W + q], a);
           out[e] = a;
         }
       }
@@ -469,7 +481,7 @@ __device__ void update_stream(cpx<T> *__restrict__ X, int ld, int rows, const in
       int o = threadIdx.x + e * NT;
       if (o < 32 * W) {
         int q = o >> 5, r = o & 31;
-        if (q < wcnt && i0 + r < rows) X[size_t(cols[q]) * ld + i0 + r] = out[e];
+        if (cols[q] >= 0 && i0 + r < rows) X[size_t(cols[q]) * ld + i0 + r] = out[e];
       }
     }
   }
@@ -479,7 +491,7 @@ __device__ void update_stream(cpx<T> *__restrict__ X, int ld, int rows, const in
 // -- resident path (float, ell <= RES_ROWS, W == 32) ---------------------
 // Ab[r][p] = A[cols[p]][r]; eight independent loads in flight per thread.
 template <typename T, int NT, int W>
-__device__ void load_block_res(const cpx<T> *__restrict__ A, int ell, const int *cols, int wcnt, Smem<T, W> &sm) {
+__device__ void load_block_res(const cpx<T> *__restrict__ A, int ell, const int *cols, Smem<T, W> &sm) {
   constexpr int TP = W + 1, UN = 8;
   const int tot = W * ell;
   for (int base = threadIdx.x; base < tot; base += NT * UN) {
@@ -488,7 +500,7 @@ __device__ void load_block_res(const cpx<T> *__restrict__ A, int ell, const int 
     for (int u = 0; u < UN; ++u) {
       const int idx = base + u * NT;
       const int p = idx / ell, r = idx - p * ell;
-      v[u] = (idx < tot && p < wcnt) ? A[size_t(cols[p]) * ell + r] : czero<T>();
+      v[u] = (idx < tot && cols[p] >= 0) ? A[size_t(cols[p]) * ell + r] : czero<T>();
     }
 #pragma unroll
     for (int u = 0; u < UN; ++u) {
@@ -532,7 +544,7 @@ __device__ void gram_res(int ell, Smem<T, W> &sm) {
 
 // A[:, cols] <- Ab J (Ab resident): thread owns 4 rows x 8 columns.
 template <typename T, int NT, int W>
-__device__ void update_res(cpx<T> *__restrict__ A, int ell, const int *cols, int wcnt,
+__device__ void update_res(cpx<T> *__restrict__ A, int ell, const int *cols,
                            const cpx<T> *__restrict__ Jm, Smem<T, W> &sm) {
   static_assert(W == 32 && NT % 4 == 0, "resident update layout");
   constexpr int TP = W + 1, RB = NT / 4;
@@ -544,7 +556,7 @@ __device__ void update_res(cpx<T> *__restrict__ A, int ell, const int *cols, int
     for (int i = 0; i < 4; ++i)
 #pragma unroll
       for (int j = 0; j < 8; ++j) acc[i][j] = czero<T>();
-    for (int p = 0; p < wcnt; ++p) {
+    for (int p = 0; p < W; ++p) {
       cpx<T> jr[8], a[4];
 #pragma unroll
       for (int j = 0; j < 8; ++j) jr[j] = Jm[p * W + q0 + j];
@@ -564,7 +576,7 @@ __device__ void update_res(cpx<T> *__restrict__ A, int ell, const int *cols, int
       if (r < ell) {
 #pragma unroll
         for (int j = 0; j < 8; ++j)
-          if (q0 + j < wcnt) A[size_t(cols[q0 + j]) * ell + r] = acc[i][j];
+          if (cols[q0 + j] >= 0) A[size_t(cols[q0 + j]) * ell + r] = acc[i][j];
       }
     }
   }
@@ -576,7 +588,8 @@ __device__ void update_res(cpx<T> *__restrict__ A, int ell, const int *cols, int
 // rotations from the current G, then forms G' = R^H G R and J' = J R into
 // the other buffer (two barriers per round).  Returns the buffer holding J.
 template <typename T, int NT, int W>
-__device__ const cpx<T> *jacobi_gram(Smem<T, W> &sm, int wcnt, T tol, T tiny2) {
+__device__ const cpx<T> *jacobi_gram(Smem<T, W> &sm, const int *cols, T tol, T tiny2, const cpx<T> **gfinal,
+                                     int mode) {
   constexpr int H = W / 2;
   cpx<T> *Gc = sm.G, *Gn = sm.G2, *Jc = sm.J, *Jn = sm.J2;
   for (int idx = threadIdx.x; idx < W * W; idx += NT) {
@@ -584,14 +597,28 @@ __device__ const cpx<T> *jacobi_gram(Smem<T, W> &sm, int wcnt, T tol, T tiny2) {
     Jc[idx] = (p == q) ? mkc<T>(T(1), T(0)) : czero<T>();
   }
   __syncthreads();
-  for (int r = 0; r < W - 1; ++r) {
+  // mode 0: all pairs of the W vectors (W-1 rounds); mode 1: only pairs
+  // across the two halves (H rounds); mode 2: only pairs within each half
+  // (H-1 rounds).  Every round rotates H disjoint pairs.
+  const int rounds = mode == 0 ? W - 1 : (mode == 1 ? H : H - 1);
+  for (int r = 0; r < rounds; ++r) {
     if (threadIdx.x < H) {
       int t = threadIdx.x, p, q;
-      rr_pair<W>(r, t, p, q);
+      if (mode == 0) {
+        rr_pair<W>(r, t, p, q);
+      } else if (mode == 1) {
+        p = t;
+        q = H + (t + r) % H;
+      } else {
+        const int h = t / (H / 2), tt = t % (H / 2);
+        rr_pair<H>(r, tt, p, q);
+        p += h * H;
+        q += h * H;
+      }
       T c = T(1), sn = T(0);
       cpx<T> e = mkc<T>(T(1), T(0));
       bool rot = false;
-      if (q < wcnt) {
+      if (cols[p] >= 0 && cols[q] >= 0) {
         T a = Gc[p * W + p].x, b = Gc[q * W + q].x;
         cpx<T> g = Gc[p * W + q];
         T ag = sqrt(cabs2(g));
@@ -641,12 +668,16 @@ __device__ const cpx<T> *jacobi_gram(Smem<T, W> &sm, int wcnt, T tol, T tiny2) {
     Jc = Jn;
     Jn = t1;
   }
+  *gfinal = Gc;
   return Jc;
 }
 
 template <typename T, int NT, int W>
+__device__ void bitonic_desc(double *key, int *idx, int P);
+
+template <typename T, int NT, int W>
 __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps, Smem<T, W> &sm,
-                          long long *cyc) {
+                          long long *cyc, double *__restrict__ nrm, int *__restrict__ ord, int scheme) {
   using L = SmemLayout<T, W>;
   constexpr int B = W / 2;
   const bool resident = (L::RES_ROWS > 0) && ell <= L::RES_ROWS;
@@ -660,50 +691,99 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
   double fro = 0.0;
   for (size_t idx = threadIdx.x; idx < size_t(ell) * c; idx += NT) {
     cpx<T> x = A[idx];
-    fro += double(x.x) * x.x + double(x.y) * x.y;
+    fro += double(x.x * x.x + x.y * x.y);
   }
   fro = block_sum<NT>(fro, sm.red);
   const T tiny2 = T(fro * double(Eps<T>::v) * double(Eps<T>::v));
   const int nblk = (c + B - 1) / B;
   int *cols = sm.ired + 128;  // W ints (ired[0..128) is reduction scratch)
+  // Column norms^2, kept current from the rotated Gram diagonals; each sweep
+  // visits the columns in decreasing-norm order (de Rijk's ordering), which
+  // shortens the one-sided Jacobi iteration.
+  if (nblk > 2) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int j = warp; j < c; j += NT / 32) {
+      T part = T(0);
+      for (int i = lane; i < ell; i += 32) part += cabs2(A[size_t(j) * ell + i]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+      if (lane == 0) nrm[j] = double(part);
+    }
+    __syncthreads();
+  }
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     int rotated = 0;
-    const int npairs = (nblk <= 2) ? 1 : nblk * (nblk - 1) / 2;
-    int I = 0, Jb = 1;
-    for (int pr = 0; pr < npairs; ++pr) {
-      int wcnt, wi = 0, wj = 0;
-      if (nblk <= 2) {
-        wcnt = c;
-      } else {
-        wi = min(B, c - I * B);
-        wj = min(B, c - Jb * B);
-        wcnt = wi + wj;
+    if (nblk > 2) {
+      int P = 1;
+      while (P < c) P <<= 1;
+      double *key = reinterpret_cast<double *>(sm.r0);
+      int *kidx = reinterpret_cast<int *>(key + P);
+      for (int j = threadIdx.x; j < P; j += NT) {
+        key[j] = j < c ? nrm[j] : -1.0;
+        kidx[j] = j;
       }
+      __syncthreads();
+      bitonic_desc<T, NT, W>(key, kidx, P);
+      for (int j = threadIdx.x; j < c; j += NT) ord[j] = kidx[j];
+      __syncthreads();
+    }
+    // Steps of one sweep: nblk <= 2 -> one step over all c vectors (every
+    // pair).  Otherwise every pair is visited once: ceil(nblk/2) steps over
+    // block pairs (2b, 2b+1) rotating only pairs inside each block, then one
+    // step per block pair I < J rotating only pairs across the two blocks.
+    // Slots [0, B) hold block I, [B, W) block J; cols[t] = -1 marks an empty slot.
+    const int ndiag = (nblk <= 2 || scheme == 0) ? 0 : (nblk + 1) / 2;
+    const int nsteps = (nblk <= 2) ? 1 : ndiag + nblk * (nblk - 1) / 2;
+    int I = 0, Jb = 1;
+    for (int st = 0; st < nsteps; ++st) {
+      int mode, bi, bj;
+      if (nblk <= 2) {
+        mode = 0;
+        bi = 0;
+        bj = 1;
+      } else if (st < ndiag) {
+        mode = 2;
+        bi = 2 * st;
+        bj = (2 * st + 1 < nblk) ? 2 * st + 1 : -1;
+      } else {
+        mode = scheme == 0 ? 0 : 1;
+        bi = I;
+        bj = Jb;
+        if (++Jb >= nblk) {
+          ++I;
+          Jb = I + 1;
+        }
+      }
+      const int wi = min(B, c - bi * B), wj = bj >= 0 ? max(0, min(B, c - bj * B)) : 0;
       if (threadIdx.x < W) {
         const int t = threadIdx.x;
-        int col = 0;
-        if (nblk <= 2)
-          col = t < c ? t : 0;
-        else
-          col = (t < wi) ? I * B + t : ((t - wi) < wj ? Jb * B + (t - wi) : 0);
+        int col = -1;
+        if (t < B) {
+          if (t < wi) col = (nblk > 2) ? ord[bi * B + t] : bi * B + t;
+        } else if (t - B < wj) {
+          col = (nblk > 2) ? ord[bj * B + (t - B)] : bj * B + (t - B);
+        }
         cols[t] = col;
       }
       __syncthreads();
       long long t0 = clock64();
       if constexpr (L::RES_ROWS > 0) {
         if (resident) {
-          load_block_res<T, NT, W>(A, ell, cols, wcnt, sm);
+          load_block_res<T, NT, W>(A, ell, cols, sm);
           gram_res<T, NT, W>(ell, sm);
         } else {
-          gram_stream<T, NT, W>(A, ell, cols, wcnt, sm);
+          gram_stream<T, NT, W>(A, ell, cols, sm);
         }
       } else {
-        gram_stream<T, NT, W>(A, ell, cols, wcnt, sm);
+        gram_stream<T, NT, W>(A, ell, cols, sm);
       }
       int need = 0;
       for (int idx = threadIdx.x; idx < W * W; idx += NT) {
         int p = idx / W, q = idx % W;
-        if (p < q && q < wcnt) {
+        if (p < q && cols[p] >= 0 && cols[q] >= 0) {
+          const bool cross = (p < B) != (q < B);
+          if (mode == 1 && !cross) continue;
+          if (mode == 2 && cross) continue;
           T a = sm.G[p * W + p].x, b = sm.G[q * W + q].x;
           T ag = sqrt(cabs2(sm.G[idx]));
           if (a > tiny2 && b > tiny2 && ag > tol * sqrt(a) * sqrt(b)) need = 1;
@@ -715,23 +795,22 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
       cyc[3] += 1;
       if (need) {
         rotated = 1;
-        const cpx<T> *Jm = jacobi_gram<T, NT, W>(sm, wcnt, tol, tiny2);
+        const cpx<T> *Gfin = nullptr;
+        const cpx<T> *Jm = jacobi_gram<T, NT, W>(sm, cols, tol, tiny2, &Gfin, mode);
         long long t2 = clock64();
         cyc[1] += t2 - t1;
         t1 = t2;
         if constexpr (L::RES_ROWS > 0) {
           if (resident)
-            update_res<T, NT, W>(A, ell, cols, wcnt, Jm, sm);
+            update_res<T, NT, W>(A, ell, cols, Jm, sm);
           else
-            update_stream<T, NT, W>(A, ell, ell, cols, wcnt, Jm, sm);
+            update_stream<T, NT, W>(A, ell, ell, cols, Jm, sm);
         } else {
-          update_stream<T, NT, W>(A, ell, ell, cols, wcnt, Jm, sm);
+          update_stream<T, NT, W>(A, ell, ell, cols, Jm, sm);
         }
+        if (nblk > 2 && threadIdx.x < W && cols[threadIdx.x] >= 0)
+          nrm[cols[threadIdx.x]] = double(Gfin[threadIdx.x * (W + 1)].x);
         cyc[2] += clock64() - t1;
-      }
-      if (++Jb >= nblk) {
-        ++I;
-        Jb = I + 1;
       }
     }
     if (!rotated) return sweep + 1;
@@ -834,14 +913,12 @@ __device__ void finalize_bond(const TrajDev &tr, int k, cpx<T> *__restrict__ gk,
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // vector norms (float64 accumulation)
   for (int j = warp; j < P; j += NT / 32) {
-    double acc = 0.0;
+    T part = T(0);  // per-lane partial in the working precision, lanes summed in float64
     if (j < c) {
       const cpx<T> *a = wk.A + size_t(j) * ell;
-      for (int i = lane; i < ell; i += 32) {
-        cpx<T> x = a[i];
-        acc += double(x.x) * double(x.x) + double(x.y) * double(x.y);
-      }
+      for (int i = lane; i < ell; i += 32) part += cabs2(a[i]);
     }
+    double acc = double(part);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) {
@@ -890,11 +967,17 @@ __device__ void finalize_bond(const TrajDev &tr, int k, cpx<T> *__restrict__ gk,
     part2 += s * s;
   }
   const double norm2 = sqrt(block_sum<NT>(part2, sm.red));
+  // Per-value factors in the working precision (float64 only for these few
+  // scalars): kept Schmidt values s2 (float64, stored as Lambda_k), 1/sigma,
+  // 1/sigma^2 and s2^2 as T.
   for (int j = threadIdx.x; j < rank; j += NT) {
     double s1 = key[j] / norm1;
-    wk.s2[j] = s1 / norm2;
-    wk.sig[j] = key[j];
+    double s2 = s1 / norm2;
+    wk.s2[j] = s2;
     wk.perm[j] = pidx[j];
+    wk.isig[j] = T(1.0 / key[j]);
+    wk.isig2[j] = T(1.0 / (key[j] * key[j]));
+    wk.w2[j] = T(s2 * s2);
   }
   // scl[0..cL): 1/Lambda_{k-1}[v]; scl[cap..cap+cR): norm2/Lambda_{k+1}[w]
   T *sclL = wk.scl, *sclR = wk.scl + tr.cap;
@@ -903,13 +986,14 @@ __device__ void finalize_bond(const TrajDev &tr, int k, cpx<T> *__restrict__ gk,
   __syncthreads();
   const int m = 2 * cL, nc = 2 * cR;
   const cpx<T> *A = wk.A, *T0 = wk.T0;
-  const double *sig = wk.sig;
+  const T *isig = wk.isig, *isig2 = wk.isig2, *w2 = wk.w2;
+  const T *lLf = wk.lam3, *lRf = wk.lam3 + 2 * tr.cap;
   const int *perm = wk.perm;
   if (colmode) {
     // vectors = columns: U[:, j] = a_src / sigma (direct)
     for (size_t idx = threadIdx.x; idx < size_t(m) * rank; idx += NT) {
       int i = int(idx / rank), j = int(idx % rank);
-      gk[idx] = cscale(A[size_t(perm[j]) * ell + i], T(1.0 / sig[j]) * sclL[i >> 1]);
+      gk[idx] = cscale(A[size_t(perm[j]) * ell + i], isig[j] * sclL[i >> 1]);
     }
     // Vh[j][col] = sum_i conj(a_src[i]) theta[i][col] / sigma^2 (recovered)
     gemm_nt<T, NT, W>(
@@ -919,15 +1003,12 @@ __device__ void finalize_bond(const TrajDev &tr, int k, cpx<T> *__restrict__ gk,
           return mkc<T>(a.x, -a.y);
         },
         [&](int col, int i) { return T0[size_t(col) * m + i]; },
-        [&](int j, int col, cpx<T> v) {
-          gk1[size_t(j) * nc + col] = cscale(v, T(1.0 / (sig[j] * sig[j])) * sclR[col % cR]);
-        },
-        sm);
+        [&](int j, int col, cpx<T> v) { gk1[size_t(j) * nc + col] = cscale(v, isig2[j] * sclR[col % cR]); }, sm);
   } else {
     // vectors = rows: Vh[j, :] = w_src / sigma (direct)
     for (size_t idx = threadIdx.x; idx < size_t(rank) * nc; idx += NT) {
       int j = int(idx / nc), col = int(idx % nc);
-      gk1[idx] = cscale(A[size_t(perm[j]) * ell + col], T(1.0 / sig[j]) * sclR[col % cR]);
+      gk1[idx] = cscale(A[size_t(perm[j]) * ell + col], isig[j] * sclR[col % cR]);
     }
     // U[i][j] = sum_col theta[i][col] conj(w_src[col]) / sigma^2 (recovered)
     gemm_nt<T, NT, W>(
@@ -936,24 +1017,23 @@ __device__ void finalize_bond(const TrajDev &tr, int k, cpx<T> *__restrict__ gk,
           cpx<T> a = A[size_t(perm[j]) * ell + col];
           return mkc<T>(a.x, -a.y);
         },
-        [&](int i, int j, cpx<T> v) { gk[size_t(i) * rank + j] = cscale(v, T(1.0 / (sig[j] * sig[j])) * sclL[i >> 1]); },
-        sm);
+        [&](int i, int j, cpx<T> v) { gk[size_t(i) * rank + j] = cscale(v, isig2[j] * sclL[i >> 1]); }, sm);
   }
   __syncthreads();
-  // local_renormalize(k) and (k+1) with the new Lambda_k = s2
-  double nk = 0.0, nk1 = 0.0;
+  // local_renormalize(k) and (k+1) with the new Lambda_k = s2: per-thread
+  // partial sums in the working precision, the block reduction in float64
+  T pk = T(0), pk1 = T(0);
   for (size_t idx = threadIdx.x; idx < size_t(m) * rank; idx += NT) {
     int i = int(idx / rank), j = int(idx % rank);
-    double l = lamL[i >> 1], s = wk.s2[j];
-    cpx<T> g = gk[idx];
-    nk += (double(g.x) * g.x + double(g.y) * g.y) * (l * l) * (s * s);
+    T l = lLf[i >> 1];
+    pk += cabs2(gk[idx]) * (l * l) * w2[j];
   }
   for (size_t idx = threadIdx.x; idx < size_t(rank) * nc; idx += NT) {
     int j = int(idx / nc), w = int(idx % nc) % cR;
-    double l = lamR[w], s = wk.s2[j];
-    cpx<T> g = gk1[idx];
-    nk1 += (double(g.x) * g.x + double(g.y) * g.y) * (s * s) * (l * l);
+    T l = lRf[w];
+    pk1 += cabs2(gk1[idx]) * w2[j] * (l * l);
   }
+  double nk = double(pk), nk1 = double(pk1);
   block_sum2<NT>(nk, nk1, sm.red);
   const T ik = T(1.0 / sqrt(nk)), ik1 = T(1.0 / sqrt(nk1));
   for (size_t idx = threadIdx.x; idx < size_t(m) * rank; idx += NT) gk[idx] = cscale(gk[idx], ik);
@@ -1015,16 +1095,16 @@ __device__ bool cholesky_lower(cpx<T> *__restrict__ S, int n, double rel, double
 // far from orthonormal rows for the factorisation to be accurate.
 template <typename T, int NT, int W>
 __device__ bool refactor_lq(const cpx<T> *__restrict__ gk, const cpx<T> *__restrict__ gk1,
-                            const double *__restrict__ lamL, const double *__restrict__ lamM,
-                            const double *__restrict__ lamR, int cL, int cM, int cR, int cap, Work<T> &wk,
+                            const T *__restrict__ lamL, const T *__restrict__ lamM,
+                            const T *__restrict__ lamR, int cL, int cM, int cR, int cap, Work<T> &wk,
                             Smem<T, W> &sm) {
   const int m = 2 * cL, nc = 2 * cR;
   cpx<T> *S = wk.A + size_t(2) * cap * cap;  // chiM x chiM, after M's m x chiM region
   // S = B B^H
   gemm_nt<T, NT, W>(
-      cM, cM, nc, [&](int x, int col) { return cscale(gk1[size_t(x) * nc + col], T(lamR[col % cR])); },
+      cM, cM, nc, [&](int x, int col) { return cscale(gk1[size_t(x) * nc + col], lamR[col % cR]); },
       [&](int y, int col) {
-        cpx<T> b = cscale(gk1[size_t(y) * nc + col], T(lamR[col % cR]));
+        cpx<T> b = cscale(gk1[size_t(y) * nc + col], lamR[col % cR]);
         return mkc<T>(b.x, -b.y);
       },
       [&](int x, int y, cpx<T> v) { S[size_t(x) * cM + y] = v; }, sm);
@@ -1034,7 +1114,7 @@ __device__ bool refactor_lq(const cpx<T> *__restrict__ gk, const cpx<T> *__restr
   cpx<T> *A = wk.A;
   gemm_nt<T, NT, W>(
       m, cM, cM,
-      [&](int i, int u) { return cscale(gk[size_t(i) * cM + u], T(lamL[i >> 1] * lamM[u])); },
+      [&](int i, int u) { return cscale(gk[size_t(i) * cM + u], lamL[i >> 1] * lamM[u]); },
       [&](int j, int u) { return u >= j ? S[size_t(u) * cM + j] : czero<T>(); },
       [&](int i, int j, cpx<T> v) { A[size_t(j) * m + i] = v; }, sm);
   return true;
@@ -1042,7 +1122,7 @@ __device__ bool refactor_lq(const cpx<T> *__restrict__ gk, const cpx<T> *__restr
 
 // One bond operation on (k, k+1): gate != nullptr -> apply_unitary2, else local_refactor.
 template <typename T, int NT, int W>
-__device__ void bond_op(const TrajDev &tr, int k, const double *gate, Work<T> &wk, int max_sweeps,
+__device__ void bond_op(const TrajDev &tr, int k, const double *gate, Work<T> &wk, int max_sweeps, int scheme,
                         Smem<T, W> &sm) {
   const int cL = tr.chi[k], cM = tr.chi[k + 1], cR = tr.chi[k + 2];
   const int m = 2 * cL, nc = 2 * cR;
@@ -1050,13 +1130,20 @@ __device__ void bond_op(const TrajDev &tr, int k, const double *gate, Work<T> &w
   const double *lamL = lam_slot(tr, k), *lamR = lam_slot(tr, k + 2);
   double *lamM = lam_slot(tr, k + 1);
   long long c0 = clock64();
+  // Lambda_{k-1}, Lambda_k, Lambda_{k+1} in the working precision (the state
+  // keeps them in float64; the contraction multiplies in T)
+  T *lLt = wk.lam3, *lMt = wk.lam3 + tr.cap, *lRt = wk.lam3 + 2 * tr.cap;
+  for (int v = threadIdx.x; v < cL; v += NT) lLt[v] = T(lamL[v]);
+  for (int u = threadIdx.x; u < cM; u += NT) lMt[u] = T(lamM[u]);
+  for (int w = threadIdx.x; w < cR; w += NT) lRt[w] = T(lamR[w]);
+  __syncthreads();
   // Refactors of a bond whose theta has more columns than its rank bound
   // chiM go through the LQ-reduced matrix M (m x chiM); gates and small
   // bonds take the direct path on theta.
   bool lq = false;
   if (!gate && cM < nc && cM <= m) {
-    build_theta<T, NT, W>(gk, gk1, lamL, lamM, lamR, cL, cM, cR, nullptr, wk.T0, wk.T0, true, sm);
-    lq = refactor_lq<T, NT, W>(gk, gk1, lamL, lamM, lamR, cL, cM, cR, tr.cap, wk, sm);
+    build_theta<T, NT, W>(gk, gk1, lLt, lMt, lRt, cL, cM, cR, nullptr, wk.T0, wk.T0, true, sm);
+    lq = refactor_lq<T, NT, W>(gk, gk1, lLt, lMt, lRt, cL, cM, cR, tr.cap, wk, sm);
   }
   bool colmode;
   int ell, c;
@@ -1068,11 +1155,11 @@ __device__ void bond_op(const TrajDev &tr, int k, const double *gate, Work<T> &w
     colmode = m > nc;  // square: vectors = rows (coalesced theta stores)
     ell = colmode ? m : nc;
     c = colmode ? nc : m;
-    build_theta<T, NT, W>(gk, gk1, lamL, lamM, lamR, cL, cM, cR, gate, wk.A, wk.T0, colmode, sm);
+    build_theta<T, NT, W>(gk, gk1, lLt, lMt, lRt, cL, cM, cR, gate, wk.A, wk.T0, colmode, sm);
   }
   long long c1 = clock64();
   long long cyc[4] = {0, 0, 0, 0};
-  int sw = jacobi_svd<T, NT, W>(wk.A, ell, c, max_sweeps, sm, cyc);
+  int sw = jacobi_svd<T, NT, W>(wk.A, ell, c, max_sweeps, sm, cyc, wk.sig, wk.perm, scheme);
   long long c2 = clock64();
   if (threadIdx.x == 0) {
     if (sw < 0) atomicOr(tr.status, ST_NOT_CONVERGED);
@@ -1106,14 +1193,21 @@ __device__ void site_probs(const TrajDev &tr, int k, double &p0, double &p1, Sme
   const int cL = tr.chi[k], cR = tr.chi[k + 1];
   const cpx<T> *g = gamma_slot<T>(tr, k);
   const double *lamL = lam_slot(tr, k), *lamR = lam_slot(tr, k + 1);
-  double a0 = 0.0, a1 = 0.0;
+  // squared Lambdas in the working precision (shared scratch), per-thread
+  // partial sums in T, block reduction in float64
+  T *wl2 = reinterpret_cast<T *>(sm.r0), *wr2 = wl2 + cL;
+  __syncthreads();
+  for (int v = threadIdx.x; v < cL; v += NT) wl2[v] = T(lamL[v] * lamL[v]);
+  for (int u = threadIdx.x; u < cR; u += NT) wr2[u] = T(lamR[u] * lamR[u]);
+  __syncthreads();
+  T b0 = T(0), b1 = T(0);
   const int tot = cL * 2 * cR;
   for (int idx = threadIdx.x; idx < tot; idx += NT) {
     int u = idx % cR, s = (idx / cR) & 1, v = idx / (2 * cR);
-    cpx<T> x = g[idx];
-    double w = (double(x.x) * x.x + double(x.y) * x.y) * (lamL[v] * lamL[v]) * (lamR[u] * lamR[u]);
-    if (s) a1 += w; else a0 += w;
+    T w = cabs2(g[idx]) * wl2[v] * wr2[u];
+    if (s) b1 += w; else b0 += w;
   }
+  double a0 = double(b0), a1 = double(b1);
   block_sum2<NT>(a0, a1, sm.red);
   p0 = a0;
   p1 = a1;
@@ -1194,10 +1288,10 @@ __device__ void run_program(const LaunchArgs &la, const Item &it, Work<T> &wk, S
     const Instr in = la.prog[it.off + pc];
     switch (in.op) {
       case OP_GATE:
-        bond_op<T, NT, W>(tr, in.k, la.gates + size_t(in.a) * 32, wk, la.max_sweeps, sm);
+        bond_op<T, NT, W>(tr, in.k, la.gates + size_t(in.a) * 32, wk, la.max_sweeps, la.jacobi_scheme, sm);
         break;
       case OP_REFACTOR:
-        bond_op<T, NT, W>(tr, in.k, nullptr, wk, la.max_sweeps, sm);
+        bond_op<T, NT, W>(tr, in.k, nullptr, wk, la.max_sweeps, la.jacobi_scheme, sm);
         break;
       case OP_MEAS:
         measure_site<T, NT, W>(tr, in.k, la.us[in.a], in.b, la.outcomes + in.a, la.probs + in.a, sm);

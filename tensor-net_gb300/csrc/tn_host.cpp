@@ -22,8 +22,14 @@ namespace {
 
 thread_local std::string g_last_error;
 
+}  // namespace
+
+void tn::set_last_error(const char *what, cudaError_t e) { g_last_error = std::string(what) + ": " + cudaGetErrorString(e); }
+
+namespace {
+
 int cuda_fail(cudaError_t e, const char *what) {
-  g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  tn::set_last_error(what, e);
   if (e == cudaErrorMemoryAllocation) return TN_ERR_OOM;
   if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return TN_ERR_NO_DEVICE;
   return TN_ERR_CUDA;

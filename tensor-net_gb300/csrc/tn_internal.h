@@ -84,6 +84,7 @@ struct LaunchArgs {
   void *ws;              // per-CTA workspace
   size_t ws_stride;      // bytes per CTA
   int max_sweeps;
+  int jacobi_scheme;      // 0: block pairs, all pairs per step; 1: within-block then cross-block steps
 };
 
 cudaError_t launch_run(int prec, const LaunchArgs &la, int grid, int sortP, int ws_cap, cudaStream_t st);
@@ -94,6 +95,9 @@ cudaError_t launch_reset(TrajDev *trajs, const int *list, int count, int prec, c
 cudaError_t launch_compile(const TrajDev *trajs, const int *list, int nt, const int *order, const int *gate_off,
                            const int *gate_ks, const int *meas_off, const int *meas_ks, int pcap, Instr *prog,
                            Item *items, Instr *gprog, Item *gitems, int gcap, int *gcount, cudaStream_t st);
+
+// Record the text of a failed CUDA call for tn_last_error() (thread-local).
+void set_last_error(const char *what, cudaError_t e);
 
 inline int next_pow2(int x) {
   int p = 1;
