@@ -113,6 +113,19 @@ int tn_mps_apply_unitary1(tn_mps *m, uint32_t k, const double *op,
 int tn_mps_apply_unitary2(tn_mps *m, uint32_t k, const double *op,
                           uint32_t rows, uint32_t cols);
 
+/* apply_unitary2 without any device allocation.  No counterpart in the
+ * reference: for callers that cannot allocate device memory when they apply
+ * a gate (a fixed memory plan that forbids allocation after start-up, or
+ * work around a CUDA graph capture).  Same arguments and result as
+ * tn_mps_apply_unitary2; the bond operation's scratch is a fixed 4 MiB
+ * device array shared by every call (handles with chi capacity above 128 in
+ * float64 or 256 in mixed precision are rejected with TN_ERR_CAPACITY).
+ * Calls that overlap on the GPU race on that array: order them on one
+ * stream.  The first call on a device looks up the array's address; make it
+ * before any stream capture begins. */
+int tn_mps_apply_unitary2_noalloc(tn_mps *m, uint32_t k, const double *op,
+                                  uint32_t rows, uint32_t cols);
+
 /* probs (mps.rs:1071-1076): out[0..2]. */
 int tn_mps_probs(const tn_mps *m, uint32_t k, double out[2]);
 /* prob (mps.rs:1138-1143). */

@@ -42,6 +42,7 @@ SIGNATURES = {
     "tn_mps_set_trunc": (C.c_int, [vp, P(tn_trunc)]),
     "tn_mps_apply_unitary1": (C.c_int, [vp, u32, P(dbl), u32, u32]),
     "tn_mps_apply_unitary2": (C.c_int, [vp, u32, P(dbl), u32, u32]),
+    "tn_mps_apply_unitary2_noalloc": (C.c_int, [vp, u32, P(dbl), u32, u32]),
     "tn_mps_probs": (C.c_int, [vp, u32, P(dbl)]),
     "tn_mps_prob": (C.c_int, [vp, u32, u32, P(dbl)]),
     "tn_mps_measure_prob": (C.c_int, [vp, u32, dbl, P(i32), P(dbl)]),

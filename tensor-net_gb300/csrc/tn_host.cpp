@@ -24,7 +24,9 @@ thread_local std::string g_last_error;
 
 }  // namespace
 
-void tn::set_last_error(const char *what, cudaError_t e) { g_last_error = std::string(what) + ": " + cudaGetErrorString(e); }
+void tn::set_last_error(const char *what, cudaError_t e) {
+  g_last_error = e == cudaSuccess ? std::string(what) : std::string(what) + ": " + cudaGetErrorString(e);
+}
 
 namespace {
 
@@ -761,6 +763,20 @@ int tn_mps_contract(const tn_mps *m, double *out, uint64_t cap) {
   std::memcpy(out, psi.data(), sizeof(double) * 2 * dim);
   return TN_OK;
 }
+
+}  // extern "C"
+
+int tn::mps_view(const tn_mps *m, tn::MpsView *out) {
+  if (!m || !out) return TN_ERR_INVALID_ARG;
+  out->dtraj = m->dtraj.as<TrajDev>();
+  out->n = int(m->n);
+  out->cap = int(m->cap);
+  out->prec = m->prec;
+  out->st = m->st;
+  return TN_OK;
+}
+
+extern "C" {
 
 int tn_mps_stats(tn_mps *m, double *out, int32_t reset) {
   if (!m) return TN_ERR_INVALID_ARG;

@@ -96,6 +96,18 @@ cudaError_t launch_compile(const TrajDev *trajs, const int *list, int nt, const 
                            const int *gate_ks, const int *meas_off, const int *meas_ks, int pcap, Instr *prog,
                            Item *items, Instr *gprog, Item *gitems, int gcap, int *gcount, cudaStream_t st);
 
+// Device-side view of a single-state handle (for entry points outside
+// tn_host.cpp that launch on it).
+struct MpsView {
+  TrajDev *dtraj;
+  int n, cap, prec;
+  cudaStream_t st;
+};
+}  // namespace tn
+struct tn_mps;
+namespace tn {
+int mps_view(const tn_mps *m, MpsView *out);
+
 // Record the text of a failed CUDA call for tn_last_error() (thread-local).
 void set_last_error(const char *what, cudaError_t e);
 
