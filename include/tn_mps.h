@@ -253,6 +253,51 @@ int tn_batch_last_launch_ms(tn_batch *b, float *gate_ms, float *sweep_ms);
  * CUDA events. */
 int tn_batch_stream(tn_batch *b, void **stream);
 
+/* ================= serving: continuous batching of requests ================= */
+
+/* One trajectory request: a seeded Haar brickwork trajectory (inputs from
+ * tn_gen_layer(seed, traj, layer, n, p)) of `depth` layers from |0...0>. */
+typedef struct {
+    uint32_t n;
+    tn_trunc trunc;
+    double p;
+    uint32_t depth;
+    uint64_t seed;
+    uint64_t traj;
+} tn_request;
+
+typedef struct {
+    uint64_t id;
+    uint32_t layers;
+    double final_entropy;  /* entropy_vn(n/2 - 1) after the last layer */
+    double latency_s;      /* completion - arrival, server clock */
+    double queue_s;        /* admission - arrival */
+    int32_t status;
+} tn_result;
+
+typedef struct tn_server tn_server;
+
+/* A server with an HBM arena of hbm_bytes for request state, up to max_slots
+ * requests resident at once, requests up to max_n qubits and bond capacity
+ * max_chi.  Admission (first come, first served) needs a free slot and the
+ * request's projected footprint n * cap^2 * 2 complex values + Lambdas in the
+ * arena; each tick advances every admitted request by one layer in one
+ * persistent launch and retires finished requests, freeing their memory. */
+int tn_server_create(uint64_t hbm_bytes, uint32_t max_slots, int32_t precision,
+                     uint32_t max_chi, uint32_t max_n, tn_server **out);
+int tn_server_free(tn_server *s);
+/* Seconds since the server was created (the clock of arrivals and latencies). */
+int tn_server_now(const tn_server *s, double *t);
+/* Queue a request; arrival < 0 means now.  TN_ERR_CAPACITY if it can never fit. */
+int tn_server_submit(tn_server *s, const tn_request *r, double arrival, uint64_t *id);
+/* Admit what fits, run one layer for every admitted request, retire finished ones. */
+int tn_server_tick(tn_server *s, uint32_t *n_active, uint32_t *n_done);
+/* Completed requests (up to cap). */
+int tn_server_poll(tn_server *s, tn_result *out, uint32_t cap, uint32_t *n);
+/* [0] traj-layers run, [1] seconds inside ticks, [2] ticks, [3] arena bytes in
+ * use, [4] pending, [5] active, [6] admitted, [7] completed. */
+int tn_server_stats(const tn_server *s, double *out);
+
 /* ======================= seeded synthetic inputs ======================= */
 
 /* gate::haar(2, rng) (gate.rs:888-909) given the Ginibre sample z (4x4

@@ -11,6 +11,7 @@ from ._lib import STATUS, TnError, lib, library_path
 from .batch import Batch
 from .inputs import gen_layer, gen_trajectory, ginibre, haar_u4
 from .mps import MPS, Trunc
+from .serve import Server, poisson_requests, run_poisson
 
 __all__ = ["MPS", "Trunc", "Batch", "TnError", "STATUS", "lib", "library_path", "build",
-           "gen_layer", "gen_trajectory", "ginibre", "haar_u4"]
+           "gen_layer", "gen_trajectory", "ginibre", "haar_u4", "Server", "poisson_requests", "run_poisson"]

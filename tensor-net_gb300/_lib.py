@@ -29,6 +29,15 @@ class tn_trunc(C.Structure):
     _fields_ = [("mode", i32), ("chi_max", u32), ("cutoff", dbl)]
 
 
+class tn_request(C.Structure):
+    _fields_ = [("n", u32), ("trunc", tn_trunc), ("p", dbl), ("depth", u32), ("seed", u64), ("traj", u64)]
+
+
+class tn_result(C.Structure):
+    _fields_ = [("id", u64), ("layers", u32), ("final_entropy", dbl), ("latency_s", dbl), ("queue_s", dbl),
+                ("status", i32)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "tn_status_string": (C.c_char_p, [C.c_int]),
@@ -75,6 +84,13 @@ SIGNATURES = {
     "tn_batch_stream": (C.c_int, [vp, P(vp)]),
     "tn_batch_last_launch_ms": (C.c_int, [vp, P(C.c_float), P(C.c_float)]),
     "tn_batch_set_tuning": (C.c_int, [vp, i32, i32]),
+    "tn_server_create": (C.c_int, [u64, u32, i32, u32, u32, P(vp)]),
+    "tn_server_free": (C.c_int, [vp]),
+    "tn_server_now": (C.c_int, [vp, P(dbl)]),
+    "tn_server_submit": (C.c_int, [vp, P(tn_request), dbl, P(u64)]),
+    "tn_server_tick": (C.c_int, [vp, P(u32), P(u32)]),
+    "tn_server_poll": (C.c_int, [vp, P(tn_result), u32, P(u32)]),
+    "tn_server_stats": (C.c_int, [vp, P(dbl)]),
     "tn_haar_u4": (C.c_int, [P(dbl), P(dbl)]),
     "tn_gen_layer": (C.c_int, [u64, u64, u32, u32, dbl, P(u32), P(dbl), P(u32), P(u32), P(dbl), P(u32)]),
     "tn_gen_ginibre": (C.c_int, [u64, u64, u32, u32, P(dbl)]),

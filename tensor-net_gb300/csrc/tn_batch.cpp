@@ -595,3 +595,93 @@ int tn_batch_stream(tn_batch *b, void **stream) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Engine mode for the serving loop: a batch whose slots own no memory.  The
+// caller (tn_serve.cpp) binds a slot to state memory it manages, uses the
+// ordinary step entry points on the bound slots, and rebinds the slot when
+// the request completes.
+namespace tn {
+
+tn_batch *batch_engine_create(uint32_t slots, int prec, int ws_cap, int max_n, int *status) {
+  *status = TN_OK;
+  if (slots == 0 || ws_cap < 1 || max_n < 1) {
+    *status = TN_ERR_INVALID_ARG;
+    return nullptr;
+  }
+  tn_batch *b = new tn_batch();
+  b->prec = prec;
+  b->ntraj = slots;
+  b->n_alloc.assign(slots, uint32_t(max_n));
+  b->cap.assign(slots, uint32_t(ws_cap));
+  b->h.assign(slots, TrajDev{});
+  b->slot_bytes.assign(slots, 0);
+  b->maxcap = ws_cap;
+  b->maxn = max_n;
+  b->sum_n = slots * 2;
+  auto bail = [&](int s) {
+    tn_batch_free(b);
+    *status = s;
+    return static_cast<tn_batch *>(nullptr);
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return bail(fail(e, "cudaStreamCreate"));
+  for (auto &ev : b->ev) {
+    e = cudaEventCreate(&ev);
+    if (e != cudaSuccess) return bail(fail(e, "cudaEventCreate"));
+  }
+  e = cudaMalloc(reinterpret_cast<void **>(&b->dtraj),
+                 sizeof(TrajDev) * slots + sizeof(double) * STAT_N * slots + sizeof(int) * (slots + 8));
+  if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(traj)"));
+  b->dstats = reinterpret_cast<double *>(b->dtraj + slots);
+  b->dstatus = reinterpret_cast<int *>(b->dstats + STAT_N * slots);
+  b->dcounter = b->dstatus + slots;
+  e = cudaMemsetAsync(b->dtraj, 0,
+                      sizeof(TrajDev) * slots + sizeof(double) * STAT_N * slots + sizeof(int) * (slots + 8), b->st);
+  if (e != cudaSuccess) return bail(fail(e, "init"));
+  for (uint32_t i = 0; i < slots; ++i) {
+    b->h[i].status = b->dstatus + i;
+    b->h[i].stats = b->dstats + size_t(STAT_N) * i;
+  }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
+  b->sortP = next_pow2(2 * b->maxcap);
+  b->bps = run_blocks_per_sm(prec, b->sortP);
+  b->grid_max = std::max(1, b->sms * b->bps);
+  b->ws_stride = run_work_bytes(prec, b->maxcap);
+  e = cudaMalloc(&b->ws, b->ws_stride * b->grid_max);
+  if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(workspace)"));
+  b->pcap = 4 * max_n + 8;
+  e = cudaStreamSynchronize(b->st);
+  if (e != cudaSuccess) return bail(fail(e, "init"));
+  return b;
+}
+
+// Bind slot t to the state memory in d (gamma/lam/chi, n, cap, truncation)
+// and reset it to |0...0>.  Stream-ordered; no synchronisation.
+int batch_bind(tn_batch *b, uint32_t t, const TrajDev &d) {
+  if (!b || t >= b->ntraj || d.cap > b->maxcap || d.n < 1) return TN_ERR_INVALID_ARG;
+  TrajDev &h = b->h[t];
+  h.gamma = d.gamma;
+  h.lam = d.lam;
+  h.chi = d.chi;
+  h.n = d.n;
+  h.cap = d.cap;
+  h.trunc_mode = d.trunc_mode;
+  h.chi_max = d.chi_max;
+  h.cutoff = d.cutoff;
+  b->n_alloc[t] = uint32_t(d.n);
+  b->cap[t] = uint32_t(d.cap);
+  b->maxn = std::max(b->maxn, d.n);
+  CKB(cudaMemcpyAsync(b->dtraj + t, &h, sizeof(TrajDev), cudaMemcpyHostToDevice, b->st));
+  int *dl = b->dcounter + 4 + (t & 3);  // small staging words, distinct per pending bind
+  int tt = int(t);
+  CKB(cudaMemcpyAsync(dl, &tt, sizeof(int), cudaMemcpyHostToDevice, b->st));
+  CKB(launch_reset(b->dtraj, dl, 1, b->prec, b->st));
+  return TN_OK;
+}
+
+cudaStream_t batch_stream(tn_batch *b) { return b->st; }
+
+}  // namespace tn

@@ -108,6 +108,14 @@ struct tn_mps;
 namespace tn {
 int mps_view(const tn_mps *m, MpsView *out);
 
+}  // namespace tn
+struct tn_batch;
+namespace tn {
+// Engine mode of a batch (serving): slots bound to caller-managed memory.
+tn_batch *batch_engine_create(uint32_t slots, int prec, int ws_cap, int max_n, int *status);
+int batch_bind(tn_batch *b, uint32_t t, const TrajDev &d);
+cudaStream_t batch_stream(tn_batch *b);
+
 // Record the text of a failed CUDA call for tn_last_error() (thread-local).
 void set_last_error(const char *what, cudaError_t e);
 

@@ -1,0 +1,130 @@
+"""Workload-level parity of the GPU path against the FP64 oracle.
+
+1. The plain-method workload (N=16 qubits from |0...0>, brickwork depth 32,
+   Haar U(4) gates, p=0.1, chi_max=64, cutoff 1e-12, half-chain entropy per
+   layer): the float64 GPU path must reproduce the oracle's outcomes (except
+   where |p - u| < 1e-9), probabilities and per-layer entropies to 1e-6, and
+   the final Schmidt values to 1e-6 relative above a 1e-6 floor.
+2. The precision workload's p set {0.05, 0.10, 0.15, 0.20, 0.30} at a size the
+   oracle finishes in seconds (N=16, chi_max=32, cutoff 1e-10, depth 24): the
+   errors of the float64 and of the mixed path against the oracle per p.  The
+   float64 path is held to 1e-6; the mixed path's errors are recorded (written
+   to $TN_PRECISION_REPORT when set) and bounded loosely, since the mixed path
+   stores the state in complex64.
+
+The oracle trajectories run in spawned worker processes (never forked after
+the GPU is in use).
+"""
+import json
+import os
+from concurrent.futures import ProcessPoolExecutor
+import multiprocessing as mp
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+P_SET = (0.05, 0.10, 0.15, 0.20, 0.30)
+
+
+def _oracle_run(args):
+    """FP64 oracle trajectory: per-layer entropy, records, final Schmidt values."""
+    import sys
+    root, n, chi, cutoff, layers = args
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    from oracle import mps_ref as R
+    m = R.MPS(n, R.Trunc.both(chi, cutoff))
+    ents, recs = [], []
+    for (gk, g, mk, us) in layers:
+        recs.append(R.apply_bilayer(m, gk, g, mk, us))
+        ents.append(m.entropy_vn(n // 2 - 1))
+    return ents, recs, [s.copy() for s in m.svals]
+
+
+def _pool():
+    return ProcessPoolExecutor(max_workers=min(8, os.cpu_count() or 1), mp_context=mp.get_context("spawn"))
+
+
+def _gpu_run(pkg, n, chi, cutoff, prec, trajs_layers):
+    b = pkg.Batch([n] * len(trajs_layers), [pkg.Trunc.both(chi, cutoff)] * len(trajs_layers), prec)
+    depth = len(trajs_layers[0])
+    ents = [[] for _ in trajs_layers]
+    recs = [[] for _ in trajs_layers]
+    for t in range(depth):
+        r, e = b.step(list(range(len(trajs_layers))), [tl[t] for tl in trajs_layers])
+        for i in range(len(trajs_layers)):
+            ents[i].append(float(e[i]))
+            recs[i].append(r[i])
+    svals = [[b.svals(i, bd) for bd in range(n - 1)] for i in range(len(trajs_layers))]
+    assert b.device_status() == 0
+    return ents, recs, svals
+
+
+def _compare(ref, gpu, floor=1e-6):
+    """Max errors: entropy (abs, per layer), probabilities (abs), Schmidt values
+    (relative, above floor) and whether the outcome records agree up to ties."""
+    r_ents, r_recs, r_sv = ref
+    g_ents, g_recs, g_sv = gpu
+    e_ent = max(abs(a - b) for a, b in zip(r_ents, g_ents))
+    e_p, ties, mismatch = 0.0, 0, False
+    for lr, lg in zip(r_recs, g_recs):
+        if [x[:2] for x in lr] != [x[:2] for x in lg]:
+            mismatch = True
+        for (k1, o1, p1), (k2, o2, p2) in zip(lr, lg):
+            e_p = max(e_p, abs(p1 - p2))
+    e_s = 0.0
+    for a, b in zip(r_sv, g_sv):
+        a, b = a[a > floor], b[b > floor]
+        if len(a) != len(b):
+            e_s = max(e_s, 1.0)
+            continue
+        if len(a):
+            e_s = max(e_s, float(np.max(np.abs(a - b) / a)))
+    return dict(entropy_abs=e_ent, prob_abs=e_p, schmidt_rel=e_s, records_equal=not mismatch)
+
+
+def test_plain_workload_float64_matches_oracle(pkg):
+    n, depth, p, chi, cutoff = 16, 32, 0.1, 64, 1e-12
+    trajs = [pkg.gen_trajectory(20261203, i, n, depth, p) for i in range(4)]
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    with _pool() as ex:
+        refs = list(ex.map(_oracle_run, [(root, n, chi, cutoff, t) for t in trajs]))
+    ents, recs, svals = _gpu_run(pkg, n, chi, cutoff, "f64", trajs)
+    for i in range(len(trajs)):
+        c = _compare(refs[i], (ents[i], recs[i], svals[i]))
+        assert c["records_equal"], (i, c)
+        assert c["entropy_abs"] < 1e-6, (i, c)
+        assert c["prob_abs"] < 1e-6, (i, c)
+        assert c["schmidt_rel"] < 1e-6, (i, c)
+
+
+def test_precision_per_p(pkg):
+    n, depth, chi, cutoff = 16, 24, 32, 1e-10
+    per_p = {p: [pkg.gen_trajectory(7, 100 * j + int(p * 100), n, depth, p) for j in range(2)] for p in P_SET}
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    jobs = [(root, n, chi, cutoff, t) for p in P_SET for t in per_p[p]]
+    with _pool() as ex:
+        refs = list(ex.map(_oracle_run, jobs))
+    report = {}
+    for prec in ("f64", "mixed"):
+        flat = [t for p in P_SET for t in per_p[p]]
+        ents, recs, svals = _gpu_run(pkg, n, chi, cutoff, prec, flat)
+        for idx, p in enumerate(j for j in P_SET for _ in range(2)):
+            c = _compare(refs[idx], (ents[idx], recs[idx], svals[idx]), floor=1e-6 if prec == "f64" else 1e-4)
+            key = f"{prec} p={p}"
+            prev = report.get(key)
+            report[key] = c if prev is None else {k: (max(prev[k], c[k]) if k != "records_equal" else
+                                                      (prev[k] and c[k])) for k in c}
+    out = os.environ.get("TN_PRECISION_REPORT")
+    if out:
+        with open(out, "w") as f:
+            json.dump(dict(workload=dict(n=n, depth=depth, chi_max=chi, cutoff=cutoff, trajectories_per_p=2),
+                           errors=report), f, indent=1)
+    for p in P_SET:
+        c = report[f"f64 p={p}"]
+        assert c["records_equal"] and c["entropy_abs"] < 1e-6 and c["prob_abs"] < 1e-6, (p, c)
+        m = report[f"mixed p={p}"]
+        if m["records_equal"]:
+            assert m["entropy_abs"] < 1e-2 and m["prob_abs"] < 1e-2, (p, m)
