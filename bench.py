@@ -58,6 +58,11 @@ def parse():
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=20.0)
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-hbm-gb", type=int, default=96)
+    ap.add_argument("--serve-slots", type=int, default=1024)
     return ap.parse_args()
 
 
@@ -345,6 +350,54 @@ def run_gpu(a, rank, world, local_rank):
                 ents=ents, dims=dims, sms=int(sms.value), layer_inputs=layer_inputs)
 
 
+def run_plain(a, pkg):
+    """The plain path: one trajectory at a time through the single-state API
+    (tn_mps_apply_bilayer + entropy read), on the same inputs as batch
+    trajectories 0..4 (one per p), timed on the same layer indices."""
+    t_lo = a.prefill + a.warmup
+    total, layers = 0.0, 0
+    for i in range(len(P_LIST)):
+        m = pkg.MPS.new_qubits(a.n, pkg.Trunc.both(a.chi, a.cutoff), a.prec)
+        for t in range(t_lo):
+            m.apply_bilayer(*pkg.gen_layer(a.seed, i, t, a.n, p_of(i)))
+        m.entropy_vn(a.n // 2 - 1)
+        for t in range(t_lo, t_lo + a.steps):
+            inp = pkg.gen_layer(a.seed, i, t, a.n, p_of(i))
+            t0 = time.perf_counter()
+            m.apply_bilayer(*inp)
+            m.entropy_vn(a.n // 2 - 1)  # the layer's entropy read (synchronises)
+            total += time.perf_counter() - t0
+            layers += 1
+        m.close()
+    return {"value": layers / total, "unit": UNIT,
+            "how": f"single-state API, one trajectory at a time, {layers} traj-layers (one trajectory per p, "
+                   f"layers [{t_lo}, {t_lo + a.steps})), host-timed"}
+
+
+def run_serving(a, pkg):
+    """Poisson serving window of the serving workload (arrivals at
+    --serve-rate/s, n log-uniform in [16, 128], chi_max in {64..512}, p in
+    [0.02, 0.3], depth in [2n, 4n]); latency = completion - arrival."""
+    reqs = pkg.poisson_requests(a.serve_rate, a.serve_seconds, a.seed)
+    srv = pkg.Server(int(a.serve_hbm_gb) << 30, max_slots=a.serve_slots, precision=a.prec, max_chi=512, max_n=128)
+    t0 = srv.now()
+    done, submitted = pkg.run_poisson(srv, reqs, a.serve_seconds, a.seed)
+    wall = srv.now() - t0
+    st = srv.stats()
+    srv.close()
+    lat = sorted(d["latency_s"] for d in done)
+
+    def pct(q):
+        if not lat:
+            return None
+        return float(lat[min(len(lat) - 1, int(math.ceil(q / 100.0 * len(lat))) - 1)])
+    return {"rate_per_s": a.serve_rate, "window_s": a.serve_seconds, "wall_s": wall, "submitted": submitted,
+            "admitted": int(st["admitted"]), "completed": len(done), "active_at_end": int(st["active"]),
+            "pending_at_end": int(st["pending"]), "p50_latency_s": pct(50), "p99_latency_s": pct(99),
+            "traj_layers_per_s": st["layers"] / wall if wall > 0 else None, "ticks": int(st["ticks"]),
+            "note": "latency percentiles over the requests completed inside the window"}
+
+
 def main():
     a = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -416,8 +469,18 @@ def main():
                  "meas_per_step": r["stats"]["meas"] / a.steps, "step_ms": r["step_ms"],
                  "gate_launch_ms, sweep_launch_ms": r["split"],
                  "lq_refactors_per_step": r["stats"]["lq_ops"] / a.steps,
+                 "svd_sweep_limit_hits": [r["stats"]["nonconv"], r["stats"]["nonconv_c_lq"],
+                                          r["stats"]["nonconv_c_direct"]],
                  "device_status": r["status"], "middle_bond_dims": [int(d[a.n // 2 - 1]) for d in r["dims"]]},
     }
+    if rank == 0 and world == 1 and not a.no_plain:
+        import __graft_entry__ as ge
+        pl = run_plain(a, ge.load_package())
+        out["plain_gpu"] = pl
+        out["batched_over_plain"] = r["value"] / pl["value"]
+    if rank == 0 and world == 1 and a.serve_seconds > 0:
+        import __graft_entry__ as ge
+        out["serving"] = run_serving(a, ge.load_package())
     if rank == 0 and world == 1 and not a.no_cpu:
         t = a.prefill + a.warmup
         layers = [r["layer_inputs"](t)[i] for i in range(min(r["B"], 16))]

@@ -183,7 +183,8 @@ int tn_mps_device_status(tn_mps *m, int32_t *status);
  * [2] bond operations, [3] Jacobi sweeps, [4] measurements,
  * [5] algorithmic HBM bytes, [6..10] SM cycles spent in theta build, block
  * Gram, block rotations, block update and finalisation, [11] Jacobi block
- * steps, [12] refactors done through the LQ-reduced matrix, [13..15] reserved.  reset != 0 zeroes them. */
+ * steps, [12] refactors done through the LQ-reduced matrix, [13] SVDs that hit
+ * the sweep limit, [14]/[15] sum of their vector counts (LQ / direct path).  reset != 0 zeroes them. */
 int tn_mps_stats(tn_mps *m, double *out, int32_t reset);
 
 /* ==================== batch of trajectories (batching) ==================== */

@@ -76,6 +76,10 @@ struct tn_batch {
   std::map<uint32_t, cudaGraphExec_t> graphs;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // around the gate and sweep launches
   bool ev_recorded = false;
+  cudaEvent_t ev_done = nullptr;  // end of the last host-input step (outputs in pinned memory)
+  uint32_t pending_nt = 0, pending_nm = 0;
+  bool async_step = false;        // engine mode: tn_batch_step returns before the outputs arrive
+  int grid_limit = 0;             // engine mode: CTAs per launch (0 = every resident CTA)
 };
 
 namespace {
@@ -183,8 +187,9 @@ int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P, bool timed = true) 
   la.prog = b->dgprog;
   la.nitems = 0;
   la.nitems_dev = b->dcounter + 3;
+  const int gmax = b->grid_limit > 0 ? std::min(b->grid_limit, b->grid_max) : b->grid_max;
   if (timed) CKB(cudaEventRecord(b->ev[0], b->st));
-  CKB(launch_run(b->prec, la, b->grid_max, b->sortP, b->maxcap, b->st));
+  CKB(launch_run(b->prec, la, gmax, b->sortP, b->maxcap, b->st));
   if (timed) CKB(cudaEventRecord(b->ev[1], b->st));
   // launch 2: one measurement-layer program per trajectory
   la.items = b->ditems;
@@ -192,7 +197,7 @@ int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P, bool timed = true) 
   la.nitems = int(nt);
   la.nitems_dev = nullptr;
   la.counter = b->dcounter + 2;
-  const int grid = std::min<int>(int(nt), b->grid_max);
+  const int grid = std::min<int>(int(nt), gmax);
   CKB(launch_run(b->prec, la, grid, b->sortP, b->maxcap, b->st));
   if (timed) {
     CKB(cudaEventRecord(b->ev[2], b->st));
@@ -254,6 +259,8 @@ int tn_batch_create(uint32_t ntraj, const uint32_t *ns, const tn_trunc *truncs, 
     e = cudaEventCreate(&ev);
     if (e != cudaSuccess) return bail(fail(e, "cudaEventCreate"));
   }
+  e = cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming);
+  if (e != cudaSuccess) return bail(fail(e, "cudaEventCreate"));
   e = cudaMalloc(&b->arena, std::max<size_t>(total, 256));
   if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(arena)"));
   e = cudaMalloc(reinterpret_cast<void **>(&b->dtraj), sizeof(TrajDev) * ntraj + sizeof(double) * STAT_N * ntraj +
@@ -325,6 +332,7 @@ int tn_batch_free(tn_batch *b) {
   if (b->arena) cudaFree(b->arena);
   for (auto &ev : b->ev)
     if (ev) cudaEventDestroy(ev);
+  if (b->ev_done) cudaEventDestroy(b->ev_done);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
   return TN_OK;
@@ -382,6 +390,8 @@ int tn_batch_step(tn_batch *b, const uint32_t *trajs, uint32_t nt, const uint32_
     b->pcap = need;
     b->step_nt = 0;
   }
+  // an earlier asynchronous step may still be reading the pinned block
+  if (b->async_step) CKB(cudaEventSynchronize(b->ev_done));
   if (int s = ensure_step(b, nt, ng, nm)) return s;
   StepLayout L = step_layout(b->step_nt, b->step_ng, b->step_nm);
   char *hb = reinterpret_cast<char *>(b->hstep);
@@ -415,11 +425,11 @@ int tn_batch_step(tn_batch *b, const uint32_t *trajs, uint32_t nt, const uint32_
   const size_t out_bytes = L.total - L.out_off;
   CKB(cudaMemcpyAsync(hb + L.out_off, reinterpret_cast<char *>(b->dstep) + L.out_off, out_bytes,
                       cudaMemcpyDeviceToHost, b->st));
-  CKB(cudaStreamSynchronize(b->st));
-  if (outcomes && nm) std::memcpy(outcomes, hb + L.outc, sizeof(int) * nm);
-  if (probs && nm) std::memcpy(probs, hb + L.probs, sizeof(double) * nm);
-  if (entropy) std::memcpy(entropy, hb + L.ents, sizeof(double) * nt);
-  return TN_OK;
+  CKB(cudaEventRecord(b->ev_done, b->st));
+  b->pending_nt = nt;
+  b->pending_nm = nm;
+  if (!outcomes && !probs && !entropy && b->async_step) return TN_OK;  // collected by batch_step_collect
+  return tn::batch_step_collect(b, outcomes, probs, entropy);
 }
 
 int tn_batch_device_inputs(tn_batch *b, uint32_t max_gates, uint32_t max_meas, void **d_trajs, void **d_gate_off,
@@ -603,7 +613,7 @@ int tn_batch_stream(tn_batch *b, void **stream) {
 // the request completes.
 namespace tn {
 
-tn_batch *batch_engine_create(uint32_t slots, int prec, int ws_cap, int max_n, int *status) {
+tn_batch *batch_engine_create(uint32_t slots, int prec, int ws_cap, int max_n, int grid_limit, int *status) {
   *status = TN_OK;
   if (slots == 0 || ws_cap < 1 || max_n < 1) {
     *status = TN_ERR_INVALID_ARG;
@@ -630,6 +640,10 @@ tn_batch *batch_engine_create(uint32_t slots, int prec, int ws_cap, int max_n, i
     e = cudaEventCreate(&ev);
     if (e != cudaSuccess) return bail(fail(e, "cudaEventCreate"));
   }
+  e = cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming);
+  if (e != cudaSuccess) return bail(fail(e, "cudaEventCreate"));
+  b->async_step = true;
+  b->grid_limit = grid_limit;
   e = cudaMalloc(reinterpret_cast<void **>(&b->dtraj),
                  sizeof(TrajDev) * slots + sizeof(double) * STAT_N * slots + sizeof(int) * (slots + 8));
   if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(traj)"));
@@ -649,6 +663,7 @@ tn_batch *batch_engine_create(uint32_t slots, int prec, int ws_cap, int max_n, i
   b->sortP = next_pow2(2 * b->maxcap);
   b->bps = run_blocks_per_sm(prec, b->sortP);
   b->grid_max = std::max(1, b->sms * b->bps);
+  if (grid_limit > 0) b->grid_max = std::min(b->grid_max, grid_limit);
   b->ws_stride = run_work_bytes(prec, b->maxcap);
   e = cudaMalloc(&b->ws, b->ws_stride * b->grid_max);
   if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(workspace)"));
@@ -683,5 +698,19 @@ int batch_bind(tn_batch *b, uint32_t t, const TrajDev &d) {
 }
 
 cudaStream_t batch_stream(tn_batch *b) { return b->st; }
+
+// Outputs of the last host-input step: waits for it, then copies from pinned memory.
+int batch_step_collect(tn_batch *b, int32_t *outcomes, double *probs, double *entropy) {
+  CKB(cudaEventSynchronize(b->ev_done));
+  StepLayout L = step_layout(b->step_nt, b->step_ng, b->step_nm);
+  const char *hb = reinterpret_cast<const char *>(b->hstep);
+  if (outcomes && b->pending_nm) std::memcpy(outcomes, hb + L.outc, sizeof(int) * b->pending_nm);
+  if (probs && b->pending_nm) std::memcpy(probs, hb + L.probs, sizeof(double) * b->pending_nm);
+  if (entropy && b->pending_nt) std::memcpy(entropy, hb + L.ents, sizeof(double) * b->pending_nt);
+  return TN_OK;
+}
+
+// true when the last host-input step has finished on the device
+bool batch_step_done(tn_batch *b) { return cudaEventQuery(b->ev_done) == cudaSuccess; }
 
 }  // namespace tn

@@ -1162,7 +1162,13 @@ __device__ void bond_op(const TrajDev &tr, int k, const double *gate, Work<T> &w
   int sw = jacobi_svd<T, NT, W>(wk.A, ell, c, max_sweeps, sm, cyc, wk.sig, wk.perm, scheme);
   long long c2 = clock64();
   if (threadIdx.x == 0) {
-    if (sw < 0) atomicOr(tr.status, ST_NOT_CONVERGED);
+    if (sw < 0) {
+      atomicOr(tr.status, ST_NOT_CONVERGED);
+      if (tr.stats) {
+        atomicAdd(tr.stats + STAT_NONCONV, 1.0);
+        atomicAdd(tr.stats + (lq ? STAT_NONCONV_LQ : STAT_NONCONV_DIRECT), double(c));
+      }
+    }
     if (tr.stats) {
       if (lq) atomicAdd(tr.stats + STAT_LQ_OPS, 1.0);
       const double a = double(m > nc ? m : nc), b = double(m > nc ? nc : m);

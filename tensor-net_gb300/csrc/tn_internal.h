@@ -50,6 +50,9 @@ enum : int {
   STAT_CYC_FINAL = 10,
   STAT_BLOCK_STEPS = 11,
   STAT_LQ_OPS = 12,     // refactors done through the LQ-reduced matrix
+  STAT_NONCONV = 13,    // Jacobi SVDs that hit the sweep limit
+  STAT_NONCONV_LQ = 14,      // sum of their vector counts, LQ path
+  STAT_NONCONV_DIRECT = 15,  // sum of their vector counts, direct path
   STAT_N = 16
 };
 
@@ -112,7 +115,9 @@ int mps_view(const tn_mps *m, MpsView *out);
 struct tn_batch;
 namespace tn {
 // Engine mode of a batch (serving): slots bound to caller-managed memory.
-tn_batch *batch_engine_create(uint32_t slots, int prec, int ws_cap, int max_n, int *status);
+tn_batch *batch_engine_create(uint32_t slots, int prec, int ws_cap, int max_n, int grid_limit, int *status);
+int batch_step_collect(tn_batch *b, int32_t *outcomes, double *probs, double *entropy);
+bool batch_step_done(tn_batch *b);
 int batch_bind(tn_batch *b, uint32_t t, const TrajDev &d);
 cudaStream_t batch_stream(tn_batch *b);
 

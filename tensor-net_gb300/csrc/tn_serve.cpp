@@ -186,7 +186,7 @@ int tn_server_create(uint64_t hbm_bytes, uint32_t max_slots, int32_t precision, 
   s->max_chi = max_chi;
   s->max_n = max_n;
   int st = TN_OK;
-  s->b = batch_engine_create(max_slots, precision, int(max_chi), int(max_n), &st);
+  s->b = batch_engine_create(max_slots, precision, int(max_chi), int(max_n), 0, &st);
   if (!s->b) {
     delete s;
     return st;

@@ -243,7 +243,8 @@ class MPS:
         L.check(self._lib.tn_mps_stats(self._h, L.dptr(out), int(reset)), "stats")
         return dict(flop_theta=out[0], flop_svd=out[1], bond_ops=out[2], sweeps=out[3], meas=out[4], bytes=out[5],
                     cyc_theta=out[6], cyc_gram=out[7], cyc_rot=out[8], cyc_update=out[9], cyc_final=out[10],
-                    block_steps=out[11], lq_ops=out[12])
+                    block_steps=out[11], lq_ops=out[12], nonconv=out[13], nonconv_c_lq=out[14],
+                    nonconv_c_direct=out[15])
 
     def device_status(self) -> int:
         st = L.i32()
