@@ -236,11 +236,21 @@ int tn_batch_synchronize(tn_batch *b);
 int tn_batch_bond_dims(tn_batch *b, uint32_t t, uint32_t *out, uint32_t cap);
 int tn_batch_svals(tn_batch *b, uint32_t t, uint32_t bond, double *out, uint32_t cap,
                    uint32_t *len);
+/* Or of the device error words of every trajectory (bits: 1 SVD sweep limit
+ * hit, 2 capacity, 4 probability sum, 8 bad instruction list) and 16 when a
+ * CTA's wait for a pushed work item ran past its limit; cleared on read. */
 int tn_batch_device_status(tn_batch *b, int32_t *status);
 /* Sum of the work counters (see tn_mps_stats) over all trajectories. */
 int tn_batch_stats(tn_batch *b, double *out, int32_t reset);
 /* Device bytes held by slot t (its footprint for admission control). */
 int tn_batch_slot_bytes(tn_batch *b, uint32_t t, uint64_t *bytes);
+/* Schedule of a layer step: 1 (default) = one persistent launch in which
+ * every gate of the layer is a work item and a trajectory's measurement
+ * layer, refactor sweep and entropy read become a work item as soon as its
+ * last gate item has finished; 0 = two launches (all gate items, then all
+ * sweep programs).  Results are bit-identical; 1 removes the idle time of the
+ * barrier between the two phases.  No counterpart in the reference. */
+int tn_batch_set_schedule(tn_batch *b, int32_t schedule);
 /* Jacobi tuning of the batch (picked by the autotuner): scheme 0 visits all
  * vector pairs of each block pair of a sweep, scheme 1 visits every pair once
  * per sweep (within-block steps, then cross-block steps); max_sweeps bounds
@@ -279,11 +289,22 @@ typedef struct {
 typedef struct tn_server tn_server;
 
 /* A server with an HBM arena of hbm_bytes for request state, up to max_slots
- * requests resident at once, requests up to max_n qubits and bond capacity
- * max_chi.  Admission (first come, first served) needs a free slot and the
- * request's projected footprint n * cap^2 * 2 complex values + Lambdas in the
- * arena; each tick advances every admitted request by one layer in one
- * persistent launch and retires finished requests, freeing their memory. */
+ * requests resident at once per cost class, requests up to max_n qubits and
+ * bond capacity max_chi.  Admission (first come, first served within a class)
+ * needs a free slot and the request's projected footprint
+ * n * cap^2 * 2 complex values + Lambdas in the arena.  Requests with bond
+ * capacity <= light_chi form class 0, the rest class 1; each class advances
+ * its admitted requests one layer per persistent launch on its own stream and
+ * share of the SMs (light_ctas CTAs for class 0, the remaining SMs for class
+ * 1), independently of the other class, and retires finished requests,
+ * freeing their memory.  light_chi = 0 means 64, light_ctas = 0 means a fifth
+ * of the SMs; light_chi >= max_chi gives one class over every SM.  No
+ * counterpart in the reference (which runs trajectories one per thread,
+ * workspace/src/haar_coev_probs.rs:164). */
+int tn_server_create_classes(uint64_t hbm_bytes, uint32_t max_slots, int32_t precision,
+                             uint32_t max_chi, uint32_t max_n, uint32_t light_chi,
+                             uint32_t light_ctas, tn_server **out);
+/* tn_server_create_classes with the default classes. */
 int tn_server_create(uint64_t hbm_bytes, uint32_t max_slots, int32_t precision,
                      uint32_t max_chi, uint32_t max_n, tn_server **out);
 int tn_server_free(tn_server *s);
@@ -291,13 +312,26 @@ int tn_server_free(tn_server *s);
 int tn_server_now(const tn_server *s, double *t);
 /* Queue a request; arrival < 0 means now.  TN_ERR_CAPACITY if it can never fit. */
 int tn_server_submit(tn_server *s, const tn_request *r, double arrival, uint64_t *id);
-/* Admit what fits, run one layer for every admitted request, retire finished ones. */
+/* Launch the next layer of every idle class (after admitting what fits),
+ * wait until at least one class has finished its layer, retire the requests
+ * of that class that reached their depth and relaunch it.  n_active = requests
+ * resident after the tick, n_done = requests retired by it. */
 int tn_server_tick(tn_server *s, uint32_t *n_active, uint32_t *n_done);
 /* Completed requests (up to cap). */
 int tn_server_poll(tn_server *s, tn_result *out, uint32_t cap, uint32_t *n);
 /* [0] traj-layers run, [1] seconds inside ticks, [2] ticks, [3] arena bytes in
  * use, [4] pending, [5] active, [6] admitted, [7] completed. */
 int tn_server_stats(const tn_server *s, double *out);
+/* Admission policy within each class: 0 (default) first come, first served;
+ * 1 least estimated work first (depth * n * cap^3).  max_active0/1 bound the
+ * requests resident in class 0/1 at once (0 = every slot), which bounds the
+ * time of one layer launch of that class and so the service time of each
+ * admitted request. */
+int tn_server_set_policy(tn_server *s, int32_t policy, uint32_t max_active0, uint32_t max_active1);
+/* Class cls (0 or 1): [0] bond capacity bound, [1] CTA limit (0 = all),
+ * [2] traj-layers run, [3] launches, [4] pending, [5] active; zeros for a
+ * class the server does not have. */
+int tn_server_class_stats(const tn_server *s, uint32_t cls, double *out);
 
 /* ======================= seeded synthetic inputs ======================= */
 

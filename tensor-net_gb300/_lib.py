@@ -85,6 +85,10 @@ SIGNATURES = {
     "tn_batch_last_launch_ms": (C.c_int, [vp, P(C.c_float), P(C.c_float)]),
     "tn_batch_set_tuning": (C.c_int, [vp, i32, i32]),
     "tn_server_create": (C.c_int, [u64, u32, i32, u32, u32, P(vp)]),
+    "tn_batch_set_schedule": (C.c_int, [vp, i32]),
+    "tn_server_create_classes": (C.c_int, [u64, u32, i32, u32, u32, u32, u32, P(vp)]),
+    "tn_server_class_stats": (C.c_int, [vp, u32, P(dbl)]),
+    "tn_server_set_policy": (C.c_int, [vp, i32, u32, u32]),
     "tn_server_free": (C.c_int, [vp]),
     "tn_server_now": (C.c_int, [vp, P(dbl)]),
     "tn_server_submit": (C.c_int, [vp, P(tn_request), dbl, P(u64)]),

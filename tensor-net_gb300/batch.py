@@ -134,8 +134,13 @@ class Batch:
     def set_tuning(self, scheme: int = 0, max_sweeps: int = 40):
         L.check(self._lib.tn_batch_set_tuning(self._h, int(scheme), int(max_sweeps)), "set_tuning")
 
+    def set_schedule(self, schedule: int = 1):
+        """1: one launch per layer (sweeps pushed as their gates finish); 0: two launches."""
+        L.check(self._lib.tn_batch_set_schedule(self._h, int(schedule)), "set_schedule")
+
     def last_launch_ms(self):
-        """(gate launch ms, sweep launch ms) of the last non-graph step."""
+        """(gate launch ms, sweep launch ms) of the last non-graph step; with
+        the one-launch schedule the first is the whole launch and the second 0."""
         g, w = C.c_float(), C.c_float()
         s = L.check(self._lib.tn_batch_last_launch_ms(self._h, C.byref(g), C.byref(w)), "last_launch_ms")
         return None if s == L.TN_NONE else (g.value, w.value)

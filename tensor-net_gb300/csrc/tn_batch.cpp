@@ -41,6 +41,8 @@ uint32_t max_rank(uint32_t n) { return n / 2 >= 20 ? (1u << 20) : (1u << (n / 2)
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+constexpr int kCounters = 16;
+
 }  // namespace
 
 struct tn_batch {
@@ -69,13 +71,19 @@ struct tn_batch {
   Item *dgitems = nullptr;
   int gcap = 0;
   uint32_t sum_n = 0;
-  int *dcounter = nullptr;  // [0] gate-launch queue, [1] reset list, [2] sweep-launch queue, [3] gate count
+  // [0] queue head, [1] reset list, [2] second-launch queue, [3] gate count, [4..8) bind staging,
+  // [8] push counter, [9] queue-wait error
+  int *dcounter = nullptr;
+  int schedule = 1;  // 1: one launch per layer, sweeps pushed as gates finish; 0: two launches
+  int *drem = nullptr, *dgstart = nullptr, *dscratch = nullptr;
+  Item *ddyn = nullptr;
   // device-input mode
   void *din = nullptr;
   uint32_t din_gates = 0, din_meas = 0;
   std::map<uint32_t, cudaGraphExec_t> graphs;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // around the gate and sweep launches
   bool ev_recorded = false;
+  bool ev_one_launch = false;  // the recorded step ran the one-launch schedule
   cudaEvent_t ev_done = nullptr;  // end of the last host-input step (outputs in pinned memory)
   uint32_t pending_nt = 0, pending_nm = 0;
   bool async_step = false;        // engine mode: tn_batch_step returns before the outputs arrive
@@ -130,11 +138,24 @@ int ensure_step(tn_batch *b, uint32_t nt, uint32_t ng, uint32_t nm) {
   b->gcap = int(std::max<uint32_t>(NG, b->sum_n));
   const size_t pbytes = sizeof(Instr) * size_t(NT) * b->pcap, ibytes = sizeof(Item) * NT;
   const size_t gpbytes = sizeof(Instr) * size_t(b->gcap), gibytes = sizeof(Item) * size_t(b->gcap);
-  CKB(cudaMalloc(reinterpret_cast<void **>(&b->dprog), pbytes + ibytes + gpbytes + gibytes + 1024));
+  const size_t nbytes = sizeof(int) * NT;
+  CKB(cudaMalloc(reinterpret_cast<void **>(&b->dprog),
+                 align256(pbytes) + 2 * align256(ibytes) + align256(gpbytes) + align256(gibytes) +
+                     3 * align256(nbytes) + 256));
   char *base = reinterpret_cast<char *>(b->dprog);
-  b->ditems = reinterpret_cast<Item *>(base + align256(pbytes));
-  b->dgprog = reinterpret_cast<Instr *>(base + align256(pbytes) + align256(ibytes));
-  b->dgitems = reinterpret_cast<Item *>(base + align256(pbytes) + align256(ibytes) + align256(gpbytes));
+  size_t at = align256(pbytes);
+  auto take = [&](size_t bytes) {
+    char *q = base + at;
+    at += align256(bytes);
+    return q;
+  };
+  b->ditems = reinterpret_cast<Item *>(take(ibytes));
+  b->dgprog = reinterpret_cast<Instr *>(take(gpbytes));
+  b->dgitems = reinterpret_cast<Item *>(take(gibytes));
+  b->ddyn = reinterpret_cast<Item *>(take(ibytes));
+  b->drem = reinterpret_cast<int *>(take(nbytes));
+  b->dgstart = reinterpret_cast<int *>(take(nbytes));
+  b->dscratch = reinterpret_cast<int *>(take(nbytes));
   b->step_nt = NT;
   b->step_ng = NG;
   b->step_nm = NM;
@@ -166,11 +187,7 @@ StepPtrs ptrs_of(const StepLayout &L, char *dbase) {
 }
 
 int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P, bool timed = true) {
-  CKB(launch_compile(b->dtraj, P.list, int(nt), P.order, P.goff, P.gks, P.moff, P.mks, b->pcap, b->dprog, b->ditems,
-                     b->dgprog, b->dgitems, b->gcap, b->dcounter + 3, b->st));
-  CKB(cudaMemsetAsync(b->dcounter, 0, 3 * sizeof(int), b->st));
   LaunchArgs la{};
-  la.counter = b->dcounter;
   la.trajs = b->dtraj;
   la.gates = P.gates;
   la.us = P.us;
@@ -182,12 +199,47 @@ int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P, bool timed = true) 
   la.ws_stride = b->ws_stride;
   la.max_sweeps = b->max_sweeps;
   la.jacobi_scheme = b->scheme;
+  la.qerr = b->dcounter + 9;
+  const int gmax = b->grid_limit > 0 ? std::min(b->grid_limit, b->grid_max) : b->grid_max;
+  if (b->schedule == 1) {
+    // One launch: gate items (most expensive trajectories first), then each
+    // trajectory's sweep program as soon as its last gate item has finished.
+    CKB(cudaMemsetAsync(b->dcounter, 0, 4 * sizeof(int), b->st));
+    CKB(cudaMemsetAsync(b->dcounter + 8, 0, sizeof(int), b->st));
+    CKB(cudaMemsetAsync(b->ddyn, 0, sizeof(Item) * nt, b->st));
+    CKB(launch_compile_dd(b->dtraj, P.list, int(nt), P.order, P.goff, P.gks, P.moff, P.mks, b->pcap, b->dprog,
+                          b->ditems, b->dgprog, b->dgitems, b->gcap, b->dcounter + 3, b->dgstart, b->dscratch,
+                          b->drem, b->ddyn, b->dcounter + 8, b->st));
+    la.counter = b->dcounter;
+    la.items = b->dgitems;
+    la.nitems = 0;
+    la.nitems_dev = b->dcounter + 3;
+    la.prog = b->dprog;
+    la.gprog = b->dgprog;
+    la.rem = b->drem;
+    la.sweeps = b->ditems;
+    la.dyn = b->ddyn;
+    la.dyn_tail = b->dcounter + 8;
+    la.nsweeps = int(nt);
+    if (timed) CKB(cudaEventRecord(b->ev[0], b->st));
+    CKB(launch_run(b->prec, la, gmax, b->sortP, b->maxcap, b->st));
+    if (timed) {
+      CKB(cudaEventRecord(b->ev[1], b->st));
+      CKB(cudaEventRecord(b->ev[2], b->st));
+      b->ev_recorded = true;
+      b->ev_one_launch = true;
+    }
+    return TN_OK;
+  }
+  CKB(launch_compile(b->dtraj, P.list, int(nt), P.order, P.goff, P.gks, P.moff, P.mks, b->pcap, b->dprog, b->ditems,
+                     b->dgprog, b->dgitems, b->gcap, b->dcounter + 3, b->st));
+  CKB(cudaMemsetAsync(b->dcounter, 0, 3 * sizeof(int), b->st));
+  la.counter = b->dcounter;
   // launch 1: every gate of the layer is an independent item
   la.items = b->dgitems;
   la.prog = b->dgprog;
   la.nitems = 0;
   la.nitems_dev = b->dcounter + 3;
-  const int gmax = b->grid_limit > 0 ? std::min(b->grid_limit, b->grid_max) : b->grid_max;
   if (timed) CKB(cudaEventRecord(b->ev[0], b->st));
   CKB(launch_run(b->prec, la, gmax, b->sortP, b->maxcap, b->st));
   if (timed) CKB(cudaEventRecord(b->ev[1], b->st));
@@ -202,6 +254,7 @@ int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P, bool timed = true) 
   if (timed) {
     CKB(cudaEventRecord(b->ev[2], b->st));
     b->ev_recorded = true;
+    b->ev_one_launch = false;
   }
   return TN_OK;
 }
@@ -264,7 +317,7 @@ int tn_batch_create(uint32_t ntraj, const uint32_t *ns, const tn_trunc *truncs, 
   e = cudaMalloc(&b->arena, std::max<size_t>(total, 256));
   if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(arena)"));
   e = cudaMalloc(reinterpret_cast<void **>(&b->dtraj), sizeof(TrajDev) * ntraj + sizeof(double) * STAT_N * ntraj +
-                                                        sizeof(int) * (ntraj + 8));
+                                                        sizeof(int) * (ntraj + kCounters));
   if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(traj)"));
   b->dstats = reinterpret_cast<double *>(b->dtraj + ntraj);
   b->dstatus = reinterpret_cast<int *>(b->dstats + STAT_N * ntraj);
@@ -561,12 +614,13 @@ int tn_batch_svals(tn_batch *b, uint32_t t, uint32_t bond, double *out, uint32_t
 
 int tn_batch_device_status(tn_batch *b, int32_t *status) {
   if (!b || !status) return TN_ERR_INVALID_ARG;
-  std::vector<int> v(b->ntraj);
-  CKB(cudaMemcpyAsync(v.data(), b->dstatus, sizeof(int) * b->ntraj, cudaMemcpyDeviceToHost, b->st));
+  std::vector<int> v(b->ntraj + kCounters);
+  CKB(cudaMemcpyAsync(v.data(), b->dstatus, sizeof(int) * (b->ntraj + kCounters), cudaMemcpyDeviceToHost, b->st));
   CKB(cudaMemsetAsync(b->dstatus, 0, sizeof(int) * b->ntraj, b->st));
+  CKB(cudaMemsetAsync(b->dcounter + 9, 0, sizeof(int), b->st));
   CKB(cudaStreamSynchronize(b->st));
-  int acc = 0;
-  for (int x : v) acc |= x;
+  int acc = v[b->ntraj + 9] ? ST_QUEUE_WAIT : 0;
+  for (uint32_t i = 0; i < b->ntraj; ++i) acc |= v[i];
   *status = acc;
   return TN_OK;
 }
@@ -574,6 +628,14 @@ int tn_batch_device_status(tn_batch *b, int32_t *status) {
 int tn_batch_slot_bytes(tn_batch *b, uint32_t t, uint64_t *bytes) {
   if (!b || t >= b->ntraj || !bytes) return TN_ERR_INVALID_ARG;
   *bytes = b->slot_bytes[t];
+  return TN_OK;
+}
+
+int tn_batch_set_schedule(tn_batch *b, int32_t schedule) {
+  if (!b || schedule < 0 || schedule > 1) return TN_ERR_INVALID_ARG;
+  for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);  // captured launches follow the old schedule
+  b->graphs.clear();
+  b->schedule = schedule;
   return TN_OK;
 }
 
@@ -592,7 +654,7 @@ int tn_batch_last_launch_ms(tn_batch *b, float *gate_ms, float *sweep_ms) {
   CKB(cudaEventSynchronize(b->ev[2]));
   float g = 0.f, w = 0.f;
   CKB(cudaEventElapsedTime(&g, b->ev[0], b->ev[1]));
-  CKB(cudaEventElapsedTime(&w, b->ev[1], b->ev[2]));
+  if (!b->ev_one_launch) CKB(cudaEventElapsedTime(&w, b->ev[1], b->ev[2]));
   if (gate_ms) *gate_ms = g;
   if (sweep_ms) *sweep_ms = w;
   return TN_OK;
@@ -645,13 +707,14 @@ tn_batch *batch_engine_create(uint32_t slots, int prec, int ws_cap, int max_n, i
   b->async_step = true;
   b->grid_limit = grid_limit;
   e = cudaMalloc(reinterpret_cast<void **>(&b->dtraj),
-                 sizeof(TrajDev) * slots + sizeof(double) * STAT_N * slots + sizeof(int) * (slots + 8));
+                 sizeof(TrajDev) * slots + sizeof(double) * STAT_N * slots + sizeof(int) * (slots + kCounters));
   if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(traj)"));
   b->dstats = reinterpret_cast<double *>(b->dtraj + slots);
   b->dstatus = reinterpret_cast<int *>(b->dstats + STAT_N * slots);
   b->dcounter = b->dstatus + slots;
   e = cudaMemsetAsync(b->dtraj, 0,
-                      sizeof(TrajDev) * slots + sizeof(double) * STAT_N * slots + sizeof(int) * (slots + 8), b->st);
+                      sizeof(TrajDev) * slots + sizeof(double) * STAT_N * slots + sizeof(int) * (slots + kCounters),
+                      b->st);
   if (e != cudaSuccess) return bail(fail(e, "init"));
   for (uint32_t i = 0; i < slots; ++i) {
     b->h[i].status = b->dstatus + i;

@@ -176,21 +176,18 @@ struct SmemLayout {
     return (r + 255) & ~size_t(255);
   }
   static constexpr size_t ab_bytes = size_t(RES_ROWS) * TP * sizeof(cpx<T>);
-  static constexpr size_t g_bytes = size_t(W) * W * sizeof(cpx<T>);
+  static constexpr int GP = W + 1;                // padded row pitch of G and J
+  static constexpr size_t g_bytes = size_t(W) * GP * sizeof(cpx<T>);
   static constexpr size_t ts_bytes = size_t(32) * TP * sizeof(cpx<T>);
-  static constexpr size_t rot_bytes = size_t(W) * (2 * sizeof(cpx<T>) + 2 * sizeof(int));
   __host__ __device__ static size_t total(int P) {
-    return region0(P) + ab_bytes + 4 * g_bytes + ts_bytes + rot_bytes + 128 * sizeof(double) + 256 * sizeof(int) +
-           512;
+    return region0(P) + ab_bytes + 2 * g_bytes + ts_bytes + 128 * sizeof(double) + 256 * sizeof(int) + 512;
   }
 };
 
 template <typename T, int W>
 struct Smem {
   unsigned char *r0;
-  cpx<T> *Ab, *G, *G2, *J, *J2, *Ts;
-  cpx<T> *ca, *cb;  // per index i of a round: R[ra[i]][i], R[rb[i]][i]
-  int *ra, *rb;     // the rotation pair (p, q) containing i
+  cpx<T> *Ab, *G, *J, *Ts;  // G and J: W x W, row pitch W + 1
   double *red;
   int *ired;
   __device__ Smem(unsigned char *base, int P) {
@@ -205,22 +202,10 @@ struct Smem {
     p += L::ab_bytes;
     G = reinterpret_cast<cpx<T> *>(p);
     p += L::g_bytes;
-    G2 = reinterpret_cast<cpx<T> *>(p);
-    p += L::g_bytes;
     J = reinterpret_cast<cpx<T> *>(p);
-    p += L::g_bytes;
-    J2 = reinterpret_cast<cpx<T> *>(p);
     p += L::g_bytes;
     Ts = reinterpret_cast<cpx<T> *>(p);
     p += L::ts_bytes;
-    ca = reinterpret_cast<cpx<T> *>(p);
-    p += W * sizeof(cpx<T>);
-    cb = reinterpret_cast<cpx<T> *>(p);
-    p += W * sizeof(cpx<T>);
-    ra = reinterpret_cast<int *>(p);
-    p += W * sizeof(int);
-    rb = reinterpret_cast<int *>(p);
-    p += W * sizeof(int);
     p = al(p);
     red = reinterpret_cast<double *>(p);
     p += 128 * sizeof(double);
@@ -447,7 +432,7 @@ __device__ void gram_stream(const cpx<T> *__restrict__ A, int ell, const int *co
 #pragma unroll
   for (int e = 0; e < PER; ++e) {
     int o = threadIdx.x + e * NT;
-    if (o < W * W) sm.G[o] = acc[e];
+    if (o < W * W) sm.G[(o / W) * (W + 1) + o % W] = acc[e];
   }
   __syncthreads();
 }
@@ -471,7 +456,7 @@ __device__ void update_stream(cpx<T> *__restrict__ X, int ld, int rows, const in
         int q = o >> 5, r = o & 31;
         if (cols[q] >= 0) {
           cpx<T> a = czero<T>();
-          for (int p = 0; p < W; ++p) a = cfma(sm.Ts[r * TP + p], Jm[p * W + q], a);
+          for (int p = 0; p < W; ++p) a = cfma(sm.Ts[r * TP + p], Jm[p * (W + 1) + q], a);
           out[e] = a;
         }
       }
@@ -489,187 +474,225 @@ __device__ void update_stream(cpx<T> *__restrict__ X, int ld, int rows, const in
 }
 
 // -- resident path (float, ell <= RES_ROWS, W == 32) ---------------------
-// Ab[r][p] = A[cols[p]][r]; eight independent loads in flight per thread.
+// Slots [s0, s0 + W/2) of Ab (Ab[r][s0 + p] = A[rc[s0 + p]][r]) from A, or
+// back to A; eight independent accesses in flight per thread.  No barrier.
 template <typename T, int NT, int W>
-__device__ void load_block_res(const cpx<T> *__restrict__ A, int ell, const int *cols, Smem<T, W> &sm) {
-  constexpr int TP = W + 1, UN = 8;
-  const int tot = W * ell;
+__device__ void load_half_res(const cpx<T> *__restrict__ A, int ell, const int *rc, int s0, Smem<T, W> &sm) {
+  constexpr int TP = W + 1, B = W / 2, UN = 8;
+  const int tot = B * ell;
   for (int base = threadIdx.x; base < tot; base += NT * UN) {
     cpx<T> v[UN];
 #pragma unroll
     for (int u = 0; u < UN; ++u) {
       const int idx = base + u * NT;
       const int p = idx / ell, r = idx - p * ell;
-      v[u] = (idx < tot && cols[p] >= 0) ? A[size_t(cols[p]) * ell + r] : czero<T>();
+      v[u] = (idx < tot && rc[s0 + p] >= 0) ? A[size_t(rc[s0 + p]) * ell + r] : czero<T>();
     }
 #pragma unroll
     for (int u = 0; u < UN; ++u) {
       const int idx = base + u * NT;
       const int p = idx / ell, r = idx - p * ell;
-      if (idx < tot) sm.Ab[r * TP + p] = v[u];
+      if (idx < tot) sm.Ab[r * TP + s0 + p] = v[u];
     }
   }
-  __syncthreads();
 }
 
-// G = Ab^H Ab: warp w owns rows 2w, 2w+1 of G, lane q its column; full sums
-// over ell (no cross-warp reduction).
+template <typename T, int NT, int W>
+__device__ void store_half_res(cpx<T> *__restrict__ A, int ell, const int *rc, int s0, const Smem<T, W> &sm) {
+  constexpr int TP = W + 1, B = W / 2;
+  for (int idx = threadIdx.x; idx < B * ell; idx += NT) {
+    const int p = idx / ell, r = idx - p * ell;
+    if (rc[s0 + p] >= 0) A[size_t(rc[s0 + p]) * ell + r] = sm.Ab[r * TP + s0 + p];
+  }
+}
+
+// G = Ab^H Ab.  Warp w computes rows 8(w % 4) .. +7 of G over the rows
+// r = w / 4 (mod 4) of Ab, lane q holding column q: eight broadcast loads and
+// one row load feed 8 complex FMAs per lane and row.  The four partial sums
+// (G itself, two 32 x 32 tiles in region 0 -- free during the Jacobi steps --
+// and Ts) are then added in a fixed order.
 template <typename T, int NT, int W>
 __device__ void gram_res(int ell, Smem<T, W> &sm) {
   static_assert(W == 32 && NT == 512, "resident Gram assumes W = 32, 16 warps");
-  constexpr int TP = W + 1;
+  static_assert(SmemLayout<T, W>::theta_bytes >= 2 * W * W * sizeof(cpx<T>), "partials fit region 0");
+  constexpr int TP = W + 1, GP = W + 1, RS = 8, KS = 4;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int p0 = 2 * warp;
-  cpx<T> a0 = czero<T>(), a1 = czero<T>(), b0 = czero<T>(), b1 = czero<T>();
-  int r = 0;
-  for (; r + 1 < ell; r += 2) {
-    const cpx<T> *row = sm.Ab + r * TP;
-    cpx<T> x0 = row[p0], x1 = row[p0 + 1], y = row[lane];
-    cpx<T> u0 = row[TP + p0], u1 = row[TP + p0 + 1], z = row[TP + lane];
-    a0 = cjfma(x0, y, a0);
-    a1 = cjfma(x1, y, a1);
-    b0 = cjfma(u0, z, b0);
-    b1 = cjfma(u1, z, b1);
+  const int p0 = RS * (warp % KS), ks = warp / KS;
+  cpx<T> acc[RS];
+#pragma unroll
+  for (int i = 0; i < RS; ++i) acc[i] = czero<T>();
+  int r = ks;
+  for (; r + KS < ell; r += 2 * KS) {
+    const cpx<T> *row0 = sm.Ab + r * TP, *row1 = row0 + KS * TP;
+    cpx<T> x0[RS], x1[RS];
+#pragma unroll
+    for (int i = 0; i < RS; ++i) {
+      x0[i] = row0[p0 + i];
+      x1[i] = row1[p0 + i];
+    }
+    const cpx<T> y0 = row0[lane], y1 = row1[lane];
+#pragma unroll
+    for (int i = 0; i < RS; ++i) acc[i] = cjfma(x1[i], y1, cjfma(x0[i], y0, acc[i]));
   }
   if (r < ell) {
-    const cpx<T> *row = sm.Ab + r * TP;
-    cpx<T> x0 = row[p0], x1 = row[p0 + 1], y = row[lane];
-    a0 = cjfma(x0, y, a0);
-    a1 = cjfma(x1, y, a1);
+    const cpx<T> *row0 = sm.Ab + r * TP;
+    const cpx<T> y0 = row0[lane];
+#pragma unroll
+    for (int i = 0; i < RS; ++i) acc[i] = cjfma(row0[p0 + i], y0, acc[i]);
   }
-  sm.G[p0 * W + lane] = cadd(a0, b0);
-  sm.G[(p0 + 1) * W + lane] = cadd(a1, b1);
+  // partials 1, 2 unpadded (pitch W: 2 W^2 values fit region 0), 3 in Ts (pitch W + 1)
+  cpx<T> *r0 = reinterpret_cast<cpx<T> *>(sm.r0);
+  cpx<T> *dst = ks == 0 ? sm.G : (ks == 1 ? r0 : (ks == 2 ? r0 + W * W : sm.Ts));
+  const int pitch = (ks == 1 || ks == 2) ? W : GP;
+#pragma unroll
+  for (int i = 0; i < RS; ++i) dst[(p0 + i) * pitch + lane] = acc[i];
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < W * W; idx += NT) {
+    const int o = (idx / W) * GP + idx % W;
+    sm.G[o] = cadd(cadd(sm.G[o], r0[idx]), cadd(r0[W * W + idx], sm.Ts[o]));
+  }
   __syncthreads();
 }
 
-// A[:, cols] <- Ab J (Ab resident): thread owns 4 rows x 8 columns.
+// Ab <- Ab J in place (Ab resident, ell <= 4 * NT / 4 rows): thread owns
+// 4 rows x 8 columns, all products formed before the barrier, then stored.
 template <typename T, int NT, int W>
-__device__ void update_res(cpx<T> *__restrict__ A, int ell, const int *cols,
-                           const cpx<T> *__restrict__ Jm, Smem<T, W> &sm) {
+__device__ void update_res(int ell, const cpx<T> *__restrict__ Jm, Smem<T, W> &sm) {
   static_assert(W == 32 && NT % 4 == 0, "resident update layout");
   constexpr int TP = W + 1, RB = NT / 4;
+  static_assert(SmemLayout<T, W>::RES_ROWS <= 4 * RB, "one pass covers every resident row");
   const int qb = threadIdx.x / RB, rb = threadIdx.x % RB;
   const int q0 = qb * 8;
-  for (int r0 = 0; r0 < ell; r0 += 4 * RB) {
-    cpx<T> acc[4][8];
+  cpx<T> acc[4][8];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = czero<T>();
+  for (int p = 0; p < W; ++p) {
+    cpx<T> jr[8], a[4];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) jr[j] = Jm[p * (W + 1) + q0 + j];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int r = rb + i * RB;
+      a[i] = r < ell ? sm.Ab[r * TP + p] : czero<T>();
+    }
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int j = 0; j < 8; ++j) acc[i][j] = czero<T>();
-    for (int p = 0; p < W; ++p) {
-      cpx<T> jr[8], a[4];
+      for (int j = 0; j < 8; ++j) acc[i][j] = cfma(a[i], jr[j], acc[i][j]);
+  }
+  __syncthreads();
 #pragma unroll
-      for (int j = 0; j < 8; ++j) jr[j] = Jm[p * W + q0 + j];
+  for (int i = 0; i < 4; ++i) {
+    const int r = rb + i * RB;
+    if (r < ell) {
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        int r = r0 + rb + i * RB;
-        a[i] = r < ell ? sm.Ab[r * TP + p] : czero<T>();
-      }
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 8; ++j) acc[i][j] = cfma(a[i], jr[j], acc[i][j]);
-    }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      int r = r0 + rb + i * RB;
-      if (r < ell) {
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-          if (cols[q0 + j] >= 0) A[size_t(cols[q0 + j]) * ell + r] = acc[i][j];
-      }
+      for (int j = 0; j < 8; ++j) sm.Ab[r * TP + q0 + j] = acc[i][j];
     }
   }
   __syncthreads();
 }
 
+// Rotation of the Hermitian 2x2 [[a, g], [conj g, b]] that zeroes g
+// (Rutishauser's formulas: t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)),
+// zeta = (b - a) / 2|g|, c = 1/sqrt(1 + t^2), s = t c, e = conj(g)/|g|), or
+// false when the pair is below the threshold |g| > tol sqrt(a b) or either
+// diagonal is rounding noise.  float: the reciprocal square root and the
+// division run on the approximate special-function path (a few ulp); c and
+// s come from the same t, so the rotation stays orthogonal to rounding and
+// an error in t only leaves a residual far below the threshold.
+template <typename T>
+__device__ __forceinline__ bool jacobi_rotation(T a, T b, cpx<T> g, T tol, T tiny2, T &c, T &sn, cpx<T> &e) {
+  const T ag = sqrt(cabs2(g));
+  if (!(a > tiny2 && b > tiny2 && ag > tol * sqrt(a) * sqrt(b))) return false;
+  const T zeta = (b - a) / (T(2) * ag);
+  T t_ = T(1) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+  if (zeta < T(0)) t_ = -t_;
+  c = T(1) / sqrt(T(1) + t_ * t_);
+  sn = t_ * c;
+  e = mkc<T>(g.x / ag, -g.y / ag);  // e^{-i phi}, g = |g| e^{i phi}
+  return true;
+}
+
+template <>
+__device__ __forceinline__ bool jacobi_rotation<float>(float a, float b, cpx<float> g, float tol, float tiny2,
+                                                       float &c, float &sn, cpx<float> &e) {
+  const float g2 = fmaf(g.x, g.x, g.y * g.y);
+  if (!(a > tiny2 && b > tiny2 && g2 > (tol * tol) * (a * b))) return false;
+  const float rg = rsqrtf(g2);  // 1 / |g|
+  const float zeta = (b - a) * (0.5f * rg);
+  const float z1 = fmaf(zeta, zeta, 1.f);
+  const float t_ = copysignf(__fdividef(1.f, fabsf(zeta) + z1 * rsqrtf(z1)), zeta);
+  c = rsqrtf(fmaf(t_, t_, 1.f));
+  sn = t_ * c;
+  e = mkc<float>(g.x * rg, -g.y * rg);
+  return true;
+}
+
 // One cyclic sweep of two-sided Jacobi on the Hermitian W x W matrix in
-// sm.G with round-robin ordering.  Each round computes its W/2 disjoint
-// rotations from the current G, then forms G' = R^H G R and J' = J R into
-// the other buffer (two barriers per round).  Returns the buffer holding J.
+// sm.G (row pitch W + 1) with round-robin ordering, accumulating J (same
+// pitch).  Warp t owns rotation pair t of every round: all its lanes compute
+// the pair's rotation from G, apply R^H to rows p, q of G (lane = column),
+// then, after a barrier, R to columns p, q of G and J (lane = row).  Pairs
+// of one round are disjoint, so each element has one writer per phase.
 template <typename T, int NT, int W>
-__device__ const cpx<T> *jacobi_gram(Smem<T, W> &sm, const int *cols, T tol, T tiny2, const cpx<T> **gfinal,
-                                     int mode) {
-  constexpr int H = W / 2;
-  cpx<T> *Gc = sm.G, *Gn = sm.G2, *Jc = sm.J, *Jn = sm.J2;
+__device__ const cpx<T> *jacobi_gram(Smem<T, W> &sm, const int *cols, T tol, T tiny2, int mode) {
+  constexpr int H = W / 2, GP = W + 1;
+  static_assert(W == 32 && NT / 32 == H, "one warp per rotation pair");
+  cpx<T> *G = sm.G, *J = sm.J;
+  const int lane = threadIdx.x & 31, t = threadIdx.x >> 5;
+  // J = I (G was written before the caller's barrier; J is first read after
+  // the barrier of round 0)
   for (int idx = threadIdx.x; idx < W * W; idx += NT) {
     int p = idx / W, q = idx % W;
-    Jc[idx] = (p == q) ? mkc<T>(T(1), T(0)) : czero<T>();
+    J[p * GP + q] = (p == q) ? mkc<T>(T(1), T(0)) : czero<T>();
   }
-  __syncthreads();
   // mode 0: all pairs of the W vectors (W-1 rounds); mode 1: only pairs
   // across the two halves (H rounds); mode 2: only pairs within each half
   // (H-1 rounds).  Every round rotates H disjoint pairs.
   const int rounds = mode == 0 ? W - 1 : (mode == 1 ? H : H - 1);
   for (int r = 0; r < rounds; ++r) {
-    if (threadIdx.x < H) {
-      int t = threadIdx.x, p, q;
-      if (mode == 0) {
-        rr_pair<W>(r, t, p, q);
-      } else if (mode == 1) {
-        p = t;
-        q = H + (t + r) % H;
-      } else {
-        const int h = t / (H / 2), tt = t % (H / 2);
-        rr_pair<H>(r, tt, p, q);
-        p += h * H;
-        q += h * H;
-      }
-      T c = T(1), sn = T(0);
-      cpx<T> e = mkc<T>(T(1), T(0));
-      bool rot = false;
-      if (cols[p] >= 0 && cols[q] >= 0) {
-        T a = Gc[p * W + p].x, b = Gc[q * W + q].x;
-        cpx<T> g = Gc[p * W + q];
-        T ag = sqrt(cabs2(g));
-        if (a > tiny2 && b > tiny2 && ag > tol * sqrt(a) * sqrt(b)) {
-          T zeta = (b - a) / (T(2) * ag);
-          T t_ = T(1) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-          if (zeta < T(0)) t_ = -t_;
-          c = T(1) / sqrt(T(1) + t_ * t_);
-          sn = t_ * c;
-          e = mkc<T>(g.x / ag, -g.y / ag);  // e^{-i phi}, g = |g| e^{i phi}
-          rot = true;
-        }
-      }
-      // R on (p, q): column p = (c, -s e), column q = (s, c e); identity if no rotation
-      sm.ra[p] = p;
-      sm.rb[p] = q;
-      sm.ra[q] = p;
-      sm.rb[q] = q;
-      sm.ca[p] = rot ? mkc<T>(c, T(0)) : mkc<T>(T(1), T(0));
-      sm.cb[p] = rot ? cscale(e, -sn) : czero<T>();
-      sm.ca[q] = rot ? mkc<T>(sn, T(0)) : czero<T>();
-      sm.cb[q] = rot ? cscale(e, c) : mkc<T>(T(1), T(0));
+    int p, q;
+    if (mode == 0) {
+      rr_pair<W>(r, t, p, q);
+    } else if (mode == 1) {
+      p = t;
+      q = H + (t + r) % H;
+    } else {
+      const int h = t / (H / 2), tt = t % (H / 2);
+      rr_pair<H>(r, tt, p, q);
+      p += h * H;
+      q += h * H;
+    }
+    // R on (p, q): column p = (c, -s e), column q = (s, c e)
+    T c = T(1), sn = T(0);
+    cpx<T> e = mkc<T>(T(1), T(0));
+    bool rot = false;
+    if (cols[p] >= 0 && cols[q] >= 0)
+      rot = jacobi_rotation<T>(G[p * GP + p].x, G[q * GP + q].x, G[p * GP + q], tol, tiny2, c, sn, e);
+    __syncwarp();  // every lane has read the pivot entries before row p, q change
+    if (rot) {
+      // rows: G[p][j] <- c G[p][j] - s conj(e) G[q][j];  G[q][j] <- s G[p][j] + c conj(e) G[q][j]
+      const cpx<T> gp = G[p * GP + lane], gq = G[q * GP + lane];
+      const cpx<T> egq = cmul(mkc<T>(e.x, -e.y), gq);
+      G[p * GP + lane] = mkc<T>(c * gp.x - sn * egq.x, c * gp.y - sn * egq.y);
+      G[q * GP + lane] = mkc<T>(sn * gp.x + c * egq.x, sn * gp.y + c * egq.y);
     }
     __syncthreads();
-    // G'[i][j] = sum_{a in pair(i)} conj(R[a][i]) sum_{b in pair(j)} G[a][b] R[b][j];  J' = J R
-    for (int idx = threadIdx.x; idx < 2 * W * W; idx += NT) {
-      const bool isJ = idx >= W * W;
-      const int o = isJ ? idx - W * W : idx;
-      const int i = o / W, j = o % W;
-      const int jp = sm.ra[j], jq = sm.rb[j];
-      const cpx<T> rjp = sm.ca[j], rjq = sm.cb[j];
-      if (isJ) {
-        Jn[o] = cfma(Jc[i * W + jq], rjq, cmul(Jc[i * W + jp], rjp));
-      } else {
-        const int ip = sm.ra[i], iq = sm.rb[i];
-        const cpx<T> rip = sm.ca[i], riq = sm.cb[i];
-        cpx<T> gpj = cfma(Gc[ip * W + jq], rjq, cmul(Gc[ip * W + jp], rjp));
-        cpx<T> gqj = cfma(Gc[iq * W + jq], rjq, cmul(Gc[iq * W + jp], rjp));
-        Gn[o] = cjfma(riq, gqj, cmul(mkc<T>(rip.x, -rip.y), gpj));
-      }
+    if (rot) {
+      // columns: X[i][p] <- c X[i][p] - s e X[i][q];  X[i][q] <- s X[i][p] + c e X[i][q]
+      const int i = lane;
+      const cpx<T> gp = G[i * GP + p], gq = cmul(e, G[i * GP + q]);
+      G[i * GP + p] = mkc<T>(c * gp.x - sn * gq.x, c * gp.y - sn * gq.y);
+      G[i * GP + q] = mkc<T>(sn * gp.x + c * gq.x, sn * gp.y + c * gq.y);
+      const cpx<T> jp = J[i * GP + p], jq = cmul(e, J[i * GP + q]);
+      J[i * GP + p] = mkc<T>(c * jp.x - sn * jq.x, c * jp.y - sn * jq.y);
+      J[i * GP + q] = mkc<T>(sn * jp.x + c * jq.x, sn * jp.y + c * jq.y);
     }
     __syncthreads();
-    cpx<T> *t1 = Gc;
-    Gc = Gn;
-    Gn = t1;
-    t1 = Jc;
-    Jc = Jn;
-    Jn = t1;
   }
-  *gfinal = Gc;
-  return Jc;
+  return J;
 }
 
 template <typename T, int NT, int W>
@@ -711,9 +734,28 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
     }
     __syncthreads();
   }
+  // Resident path: Ab keeps the two half-blocks of the last step (block ids
+  // resI, resJ, columns rcols) across steps; a half is written back to A
+  // only when another block replaces it, before the sweep's re-ordering, and
+  // on return.  Consecutive steps (I, J), (I, J+1) then move one half only.
+  int *rcols = sm.ired + 128 + W;
+  int resI = -1, resJ = -1;
+  bool dirtyI = false, dirtyJ = false;
+  auto flush = [&]() {
+    if constexpr (L::RES_ROWS > 0) {
+      if (resident) {
+        if (dirtyI) store_half_res<T, NT, W>(A, ell, rcols, 0, sm);
+        if (dirtyJ) store_half_res<T, NT, W>(A, ell, rcols, B, sm);
+        __syncthreads();
+      }
+    }
+    dirtyI = dirtyJ = false;
+    resI = resJ = -1;
+  };
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     int rotated = 0;
     if (nblk > 2) {
+      flush();  // the re-ordering changes which columns a block id names
       int P = 1;
       while (P < c) P <<= 1;
       double *key = reinterpret_cast<double *>(sm.r0);
@@ -769,7 +811,18 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
       long long t0 = clock64();
       if constexpr (L::RES_ROWS > 0) {
         if (resident) {
-          load_block_res<T, NT, W>(A, ell, cols, sm);
+          const bool keepI = bi == resI, keepJ = bj >= 0 && bj == resJ;
+          if (!keepI && dirtyI) store_half_res<T, NT, W>(A, ell, rcols, 0, sm);
+          if (!keepJ && dirtyJ) store_half_res<T, NT, W>(A, ell, rcols, B, sm);
+          __syncthreads();
+          if (!keepI) load_half_res<T, NT, W>(A, ell, cols, 0, sm);
+          if (!keepJ) load_half_res<T, NT, W>(A, ell, cols, B, sm);
+          if (threadIdx.x < W) rcols[threadIdx.x] = cols[threadIdx.x];
+          __syncthreads();
+          dirtyI = dirtyI && keepI;
+          dirtyJ = dirtyJ && keepJ;
+          resI = bi;
+          resJ = bj;
           gram_res<T, NT, W>(ell, sm);
         } else {
           gram_stream<T, NT, W>(A, ell, cols, sm);
@@ -784,8 +837,8 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
           const bool cross = (p < B) != (q < B);
           if (mode == 1 && !cross) continue;
           if (mode == 2 && cross) continue;
-          T a = sm.G[p * W + p].x, b = sm.G[q * W + q].x;
-          T ag = sqrt(cabs2(sm.G[idx]));
+          T a = sm.G[p * (W + 1) + p].x, b = sm.G[q * (W + 1) + q].x;
+          T ag = sqrt(cabs2(sm.G[p * (W + 1) + q]));
           if (a > tiny2 && b > tiny2 && ag > tol * sqrt(a) * sqrt(b)) need = 1;
         }
       }
@@ -795,26 +848,31 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
       cyc[3] += 1;
       if (need) {
         rotated = 1;
-        const cpx<T> *Gfin = nullptr;
-        const cpx<T> *Jm = jacobi_gram<T, NT, W>(sm, cols, tol, tiny2, &Gfin, mode);
+        const cpx<T> *Jm = jacobi_gram<T, NT, W>(sm, cols, tol, tiny2, mode);
         long long t2 = clock64();
         cyc[1] += t2 - t1;
         t1 = t2;
         if constexpr (L::RES_ROWS > 0) {
-          if (resident)
-            update_res<T, NT, W>(A, ell, cols, Jm, sm);
-          else
+          if (resident) {
+            update_res<T, NT, W>(ell, Jm, sm);
+            dirtyI = dirtyJ = true;
+          } else {
             update_stream<T, NT, W>(A, ell, ell, cols, Jm, sm);
+          }
         } else {
           update_stream<T, NT, W>(A, ell, ell, cols, Jm, sm);
         }
         if (nblk > 2 && threadIdx.x < W && cols[threadIdx.x] >= 0)
-          nrm[cols[threadIdx.x]] = double(Gfin[threadIdx.x * (W + 1)].x);
+          nrm[cols[threadIdx.x]] = double(sm.G[threadIdx.x * (W + 2)].x);
         cyc[2] += clock64() - t1;
       }
     }
-    if (!rotated) return sweep + 1;
+    if (!rotated) {
+      flush();
+      return sweep + 1;
+    }
   }
+  flush();
   return -1;
 }
 
@@ -1288,10 +1346,10 @@ __device__ double bond_entropy(const TrajDev &tr, int b, double alpha, double *r
 }
 
 template <typename T, int NT, int W>
-__device__ void run_program(const LaunchArgs &la, const Item &it, Work<T> &wk, Smem<T, W> &sm) {
+__device__ void run_program(const LaunchArgs &la, const Instr *prog, const Item &it, Work<T> &wk, Smem<T, W> &sm) {
   const TrajDev tr = la.trajs[it.traj];
   for (int pc = 0; pc < it.len; ++pc) {
-    const Instr in = la.prog[it.off + pc];
+    const Instr in = prog[it.off + pc];
     switch (in.op) {
       case OP_GATE:
         bond_op<T, NT, W>(tr, in.k, la.gates + size_t(in.a) * 32, wk, la.max_sweeps, la.jacobi_scheme, sm);

@@ -33,6 +33,7 @@ enum : int {
   ST_CAPACITY = 2,
   ST_PROB_SUM = 4,
   ST_BAD_INSTR = 8,
+  ST_QUEUE_WAIT = 16,  // a CTA's wait for a pushed work item ran past its limit (batch-wide)
 };
 
 // Per-trajectory counters accumulated by the kernels (float64 slots).
@@ -67,8 +68,11 @@ struct TrajDev {
   double cutoff;
 };
 
+// A work item: `len` instructions from `off` of a program array, on slot
+// `traj`.  aux: for a gate item of the dependency-driven schedule, the list
+// index of its trajectory; for a pushed sweep slot, 1 once it is written.
 struct Item {
-  int traj, off, len, pad;
+  int traj, off, len, aux;
 };
 
 struct LaunchArgs {
@@ -88,7 +92,21 @@ struct LaunchArgs {
   size_t ws_stride;      // bytes per CTA
   int max_sweeps;
   int jacobi_scheme;      // 0: block pairs, all pairs per step; 1: within-block then cross-block steps
+  // Dependency-driven schedule (rem != nullptr): items[0, *nitems_dev) are
+  // gate items with programs in gprog; when the last gate item of listed
+  // trajectory i finishes, its sweep item sweeps[i] is pushed to dyn, and the
+  // queue continues with those pushed items (nsweeps of them) in push order.
+  const Instr *gprog;
+  int *rem;               // per listed trajectory: gate items not yet finished
+  const Item *sweeps;     // per listed trajectory: measurement layer + sweep + entropy program
+  Item *dyn;              // pushed sweep items (aux = 1 once written); zeroed before compile
+  int *dyn_tail;          // push counter; zeroed before compile
+  int nsweeps;
+  int *qerr;              // set to 1 when a queue wait ran past its time limit
 };
+
+// Wait limit of a CTA on a pushed queue slot (nanoseconds of %globaltimer).
+constexpr unsigned long long kQueueWaitNs = 120ull * 1000 * 1000 * 1000;
 
 cudaError_t launch_run(int prec, const LaunchArgs &la, int grid, int sortP, int ws_cap, cudaStream_t st);
 size_t run_smem_bytes(int prec, int sortP);
@@ -98,6 +116,14 @@ cudaError_t launch_reset(TrajDev *trajs, const int *list, int count, int prec, c
 cudaError_t launch_compile(const TrajDev *trajs, const int *list, int nt, const int *order, const int *gate_off,
                            const int *gate_ks, const int *meas_off, const int *meas_ks, int pcap, Instr *prog,
                            Item *items, Instr *gprog, Item *gitems, int gcap, int *gcount, cudaStream_t st);
+// Dependency-driven variant: gate items placed trajectory by trajectory in
+// `order` rank (gstart from a scan over ranks, scratch: nt ints), sweep
+// programs at sweeps[i], rem[i] = gate items of trajectory i, and trajectories
+// without gate items pushed at once.
+cudaError_t launch_compile_dd(const TrajDev *trajs, const int *list, int nt, const int *order, const int *gate_off,
+                              const int *gate_ks, const int *meas_off, const int *meas_ks, int pcap, Instr *prog,
+                              Item *sweeps, Instr *gprog, Item *gitems, int gcap, int *gcount, int *gstart,
+                              int *scratch, int *rem, Item *dyn, int *dyn_tail, cudaStream_t st);
 
 // Device-side view of a single-state handle (for entry points outside
 // tn_host.cpp that launch on it).

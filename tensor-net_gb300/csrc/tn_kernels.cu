@@ -13,19 +13,82 @@
 
 namespace tn {
 
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ int load_acquire(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void store_release(int *p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Appends the sweep item of listed trajectory i to the pushed queue (one thread).
+__device__ void push_sweep(Item *dyn, int *tail, const Item *sweeps, int i) {
+  const int slot = atomicAdd(tail, 1);
+  const Item s = sweeps[i];
+  dyn[slot].traj = s.traj;
+  dyn[slot].off = s.off;
+  dyn[slot].len = s.len;
+  store_release(&dyn[slot].aux, 1);
+}
+
+// Static schedule (la.rem == nullptr): items[0, count) in counter order.
+// Dependency-driven schedule: gate items first; a CTA that pulls an index
+// past them waits (bounded by kQueueWaitNs) for the matching pushed sweep
+// item.  Every pushed item depends only on items already pulled by running
+// CTAs, so the waits end; a wait that runs out sets qerr and the CTA moves on.
 template <typename T, int NT, int W>
 __global__ void __launch_bounds__(NT, 1) k_run(LaunchArgs la, int sortP, int ws_cap) {
   extern __shared__ __align__(256) unsigned char smem[];
-  __shared__ int s_item;
+  __shared__ Item s_item;
+  __shared__ int s_kind;  // 0 done, 1 gate / static item, 2 pushed sweep item, 3 skip
   Smem<T, W> sm(smem, sortP);
   Work<T> wk = make_work<T>(reinterpret_cast<unsigned char *>(la.ws) + size_t(blockIdx.x) * la.ws_stride, ws_cap);
+  const bool dd = la.rem != nullptr;
   for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(la.counter, 1);
+    if (threadIdx.x == 0) {
+      const int it = atomicAdd(la.counter, 1);
+      const int G = la.nitems_dev ? *la.nitems_dev : la.nitems;
+      int kind = 0;
+      if (it < G) {
+        s_item = la.items[it];
+        kind = 1;
+      } else if (dd && it < G + la.nsweeps) {
+        Item *slot = la.dyn + (it - G);
+        const unsigned long long t0 = global_ns();
+        kind = 2;
+        while (load_acquire(&slot->aux) == 0) {
+          if (global_ns() - t0 > kQueueWaitNs) {
+            atomicExch(la.qerr, 1);
+            kind = 3;
+            break;
+          }
+          __nanosleep(200);
+        }
+        if (kind == 2) s_item = Item{slot->traj, slot->off, slot->len, 0};
+      }
+      s_kind = kind;
+    }
     __syncthreads();
-    const int it = s_item;
+    const int kind = s_kind;
+    const Item item = s_item;
     __syncthreads();
-    if (it >= (la.nitems_dev ? *la.nitems_dev : la.nitems)) break;
-    run_program<T, NT, W>(la, la.items[it], wk, sm);
+    if (kind == 0) break;
+    if (kind == 3) continue;
+    if (kind == 2) __threadfence();  // acquire side for every thread of the CTA
+    run_program<T, NT, W>(la, (dd && kind == 1) ? la.gprog : la.prog, item, wk, sm);
+    if (dd && kind == 1) {
+      __threadfence();  // this thread's writes of the gate's result, visible device-wide
+      __syncthreads();
+      if (threadIdx.x == 0 && atomicSub(la.rem + item.aux, 1) == 1) push_sweep(la.dyn, la.dyn_tail, la.sweeps, item.aux);
+    }
   }
 }
 
@@ -113,6 +176,128 @@ __global__ void k_compile(const TrajDev *trajs, const int *list, int nt, const i
   items[order[i]] = Item{t, int(size_t(i) * pcap), pc, 0};
 }
 
+// First gate-queue slot of every listed trajectory when trajectories are
+// taken in `order` rank: an exclusive scan of the gate counts by rank (one
+// block; scratch holds the counts by rank).  An `order` that is not a
+// permutation of [0, nt) is replaced by the identity.
+__global__ void k_gate_slots(int nt, const int *order, const int *gate_off, int *scratch, int *gstart) {
+  __shared__ int carry, wsum[32];
+  for (int i = threadIdx.x; i < nt; i += blockDim.x) scratch[i] = 0;
+  __syncthreads();
+  int bad = 0;
+  for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+    const int r = order[i];
+    if (r < 0 || r >= nt)
+      bad = 1;
+    else
+      atomicAdd(scratch + r, 1);
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < nt; r += blockDim.x) bad |= scratch[r] != 1;
+  bad = __syncthreads_or(bad);
+  auto rank = [&](int i) { return bad ? i : order[i]; };
+  for (int i = threadIdx.x; i < nt; i += blockDim.x) scratch[rank(i)] = gate_off[i + 1] - gate_off[i];
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int base = 0; base < nt; base += blockDim.x) {
+    const int r = base + threadIdx.x;
+    const int v = r < nt ? scratch[r] : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int w = lane < nw ? wsum[lane] : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      if (lane < nw) wsum[lane] = w;  // inclusive sums over warps
+    }
+    __syncthreads();
+    const int excl = carry + (warp ? wsum[warp - 1] : 0) + x - v;
+    __syncthreads();
+    if (r < nt) scratch[r] = excl;
+    if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < nt; i += blockDim.x) gstart[i] = scratch[rank(i)];
+}
+
+// k_compile for the dependency-driven schedule: the same instruction lists,
+// with gate items at gitems[gstart[i] + j] (aux = i), the sweep program as
+// sweeps[i], rem[i] = number of gate items of trajectory i; a trajectory
+// without gate items has its sweep item pushed here.
+__global__ void k_compile_dd(const TrajDev *trajs, const int *list, int nt, const int *gate_off, const int *gate_ks,
+                             const int *meas_off, const int *meas_ks, int pcap, Instr *prog, Item *sweeps,
+                             Instr *gprog, Item *gitems, int gcap, int *gcount, const int *gstart, int *rem, Item *dyn,
+                             int *dyn_tail) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *gcount = min(gate_off[nt], gcap);
+  if (i >= nt) return;
+  const int t = list[i];
+  const int n = trajs[t].n;
+  Instr *p = prog + size_t(i) * pcap;
+  int pc = 0;
+  auto emit = [&](int op, int k, int a, int b) {
+    if (pc < pcap) p[pc] = Instr{op, k, a, b};
+    ++pc;
+  };
+  const int g0 = gate_off[i], g1 = gate_off[i + 1];
+  bool disjoint = true;
+  for (int g = g0; g < g1 && disjoint; ++g)
+    for (int h = g + 1; h < g1; ++h)
+      if (abs(gate_ks[g] - gate_ks[h]) < 2) {
+        disjoint = false;
+        break;
+      }
+  int placed = 0;
+  for (int g = g0; g < g1; ++g) {
+    const int k = gate_ks[g];
+    const bool valid = n > 1 && k >= 0 && k < n - 1;
+    const int slot = gstart[i] + (g - g0);
+    if (slot < gcap) {
+      gprog[g < gcap ? g : slot] = (disjoint && valid) ? Instr{OP_GATE, k, g, 0} : Instr{OP_NOP, 0, 0, 0};
+      gitems[slot] = Item{t, g < gcap ? g : slot, 1, i};
+      ++placed;
+    } else if (disjoint) {
+      atomicOr(trajs[t].status, ST_BAD_INSTR);
+    }
+    if (!disjoint && valid) emit(OP_GATE, k, g, 0);
+  }
+  const int m0 = meas_off[i], m1 = meas_off[i + 1];
+  int last = -1;
+  for (int j = m0; j < m1; ++j) {
+    const int k = meas_ks[j];
+    if (k < 0 || k >= n || k <= last) continue;  // host guarantees sorted unique
+    if (last >= 0)
+      for (int b = last; b < k; ++b) emit(OP_REFACTOR, b, 0, 0);
+    emit(OP_MEAS, k, j, -1);
+    last = k;
+  }
+  if (last >= 0) {
+    for (int b = last; b < n - 1; ++b) emit(OP_REFACTOR, b, 0, 0);
+    for (int b = n - 3; b >= 0; --b) emit(OP_REFACTOR, b, 0, 0);
+  }
+  if (n >= 2) emit(OP_ENTROPY, n / 2 - 1, i, 0);
+  if (pc > pcap) {  // program did not fit: run nothing, flag the trajectory
+    atomicOr(trajs[t].status, ST_BAD_INSTR);
+    pc = 0;
+  }
+  sweeps[i] = Item{t, int(size_t(i) * pcap), pc, 0};
+  rem[i] = placed;
+  if (placed == 0) {
+    __threadfence();
+    push_sweep(dyn, dyn_tail, sweeps, i);
+  }
+}
+
 // ------------------------------------------------------------- launchers
 template <typename T, int NT, int W>
 static cudaError_t launch_run_t(const LaunchArgs &la, int grid, int sortP, int ws_cap, cudaStream_t st) {
@@ -166,6 +351,17 @@ cudaError_t launch_compile(const TrajDev *trajs, const int *list, int nt, const 
   if (nt <= 0) return cudaSuccess;
   k_compile<<<(nt + 127) / 128, 128, 0, st>>>(trajs, list, nt, order, gate_off, gate_ks, meas_off, meas_ks, pcap,
                                               prog, items, gprog, gitems, gcap, gcount);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_compile_dd(const TrajDev *trajs, const int *list, int nt, const int *order, const int *gate_off,
+                              const int *gate_ks, const int *meas_off, const int *meas_ks, int pcap, Instr *prog,
+                              Item *sweeps, Instr *gprog, Item *gitems, int gcap, int *gcount, int *gstart,
+                              int *scratch, int *rem, Item *dyn, int *dyn_tail, cudaStream_t st) {
+  if (nt <= 0) return cudaSuccess;
+  k_gate_slots<<<1, 1024, 0, st>>>(nt, order, gate_off, scratch, gstart);
+  k_compile_dd<<<(nt + 127) / 128, 128, 0, st>>>(trajs, list, nt, gate_off, gate_ks, meas_off, meas_ks, pcap, prog,
+                                                 sweeps, gprog, gitems, gcap, gcount, gstart, rem, dyn, dyn_tail);
   return cudaGetLastError();
 }
 

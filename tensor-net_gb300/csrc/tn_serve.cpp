@@ -3,19 +3,27 @@
 // Requests (one seeded Haar brickwork trajectory each: n, truncation, p,
 // depth) arrive over time.  A request is admitted when a slot is free and
 // its projected state footprint (n * cap^2 * 2 complex values + Lambdas)
-// fits in the HBM arena; admission is first come, first served.  Each tick
-// runs one persistent layer launch (tn_batch_step) over every admitted
-// request -- requests of different n and chi_max share the launch -- then
-// retires the requests that reached their depth, freeing their arena range
-// and slot for the next admission.  State stays resident on the device for a
-// request's whole life.  Latency = completion time - arrival time on the
-// server clock.
+// fits in the HBM arena; within a cost class, admission is first come, first
+// served, or least estimated work first (tn_server_set_policy), optionally
+// under a cap on the class's resident requests.  Requests of one class share
+// a layer launch (tn_batch_step) -- n and
+// chi_max may differ inside it -- and the launch's duration is that of its
+// most expensive member, so cheap requests are kept apart from expensive
+// ones: class 0 holds requests whose bond capacity is at most `light_chi`,
+// class 1 the rest.  Each class owns a batch engine with its own stream and a
+// fixed share of the SMs (its CTA limit), and the classes step independently:
+// a tick launches the next layer of every idle class, waits until at least
+// one class finishes its layer, retires the requests that reached their
+// depth (freeing arena range and slot) and relaunches that class at once.
+// State stays resident on the device for a request's whole life.
+// Latency = completion time - arrival time on the server clock.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <deque>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "tn_internal.h"
@@ -97,26 +105,40 @@ struct Active {
   double entropy = 0;
 };
 
+// One cost class: an engine (slots bound to arena memory), its queue, and
+// the staging of the layer in flight.
+struct Class {
+  tn_batch *b = nullptr;
+  uint32_t cap_max = 0;  // requests with cap_of(r) <= cap_max (and above the previous class's)
+  int ctas = 0;          // CTA limit of its launches (0 = every resident CTA)
+  std::deque<Pending> pending;
+  std::vector<Active> act;
+  std::vector<uint32_t> free_slots;
+  uint32_t max_active = 0;  // 0 = every slot
+  uint32_t active = 0;
+  bool inflight = false;
+  std::vector<uint32_t> trajs, goff, gks, moff, mks;
+  std::vector<double> gates, us, ents;
+  std::vector<uint32_t> gk, mk;
+  std::vector<double> g, u;
+  double layers = 0, launches = 0;
+};
+
 }  // namespace
 
 struct tn_server {
-  tn_batch *b = nullptr;
   int prec = TN_PREC_MIXED;
   uint32_t slots = 0, max_chi = 1, max_n = 1;
   void *arena = nullptr;
   size_t arena_bytes = 0;
   Arena alloc;
-  std::deque<Pending> pending;
-  std::vector<Active> act;
-  std::vector<uint32_t> free_slots;
+  Class cls[2];
+  int ncls = 1;
+  int policy = 0;  // 0: first come, first served; 1: least estimated work first
   std::deque<tn_result> done;
   uint64_t next_id = 1;
   double layers_done = 0, busy_s = 0, ticks = 0, admitted = 0, completed = 0;
   std::chrono::steady_clock::time_point t0;
-  // per-tick staging
-  std::vector<uint32_t> trajs, goff, gks, moff, mks;
-  std::vector<double> gates, us, probs, ents;
-  std::vector<int32_t> outc;
   double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
 };
 
@@ -128,15 +150,41 @@ size_t footprint(const tn_server *s, const tn_request &r, uint32_t cap) {
          align256(sizeof(int) * (r.n + 1));
 }
 
-int admit(tn_server *s) {
-  while (!s->pending.empty() && !s->free_slots.empty()) {
-    const Pending &p = s->pending.front();
+int class_of(const tn_server *s, const tn_request &r) {
+  return (s->ncls > 1 && cap_of(r) > s->cls[0].cap_max) ? 1 : 0;
+}
+
+// Estimated work of a request: layers x bond operations per layer (n/2
+// gates + about 2n refactors) x cap^3 (the SVD cost of a saturated bond).
+double est_work(const tn_request &r) {
+  const double c = double(cap_of(r));
+  return double(r.depth) * 2.5 * double(r.n) * c * c * c;
+}
+
+size_t pick(const tn_server *s, const Class &c) {
+  if (s->policy == 0) return 0;
+  size_t best = 0;
+  double bw = est_work(c.pending[0].r);
+  for (size_t i = 1; i < c.pending.size(); ++i) {
+    const double w = est_work(c.pending[i].r);
+    if (w < bw) {
+      bw = w;
+      best = i;
+    }
+  }
+  return best;
+}
+
+int admit(tn_server *s, Class &c) {
+  while (!c.pending.empty() && !c.free_slots.empty() && (c.max_active == 0 || c.active < c.max_active)) {
+    const size_t pi = pick(s, c);
+    const Pending p = c.pending[pi];
     const uint32_t cap = cap_of(p.r);
     const size_t bytes = footprint(s, p.r, cap);
     size_t off = 0;
-    if (!s->alloc.alloc(bytes, &off)) break;  // first come, first served: wait for memory
-    const uint32_t slot = s->free_slots.back();
-    s->free_slots.pop_back();
+    if (!s->alloc.alloc(bytes, &off)) break;  // in policy order: wait for memory
+    const uint32_t slot = c.free_slots.back();
+    c.free_slots.pop_back();
     TrajDev d{};
     char *base = static_cast<char *>(s->arena) + off;
     const size_t eb = s->prec == TN_PREC_F64 ? 16 : 8;
@@ -148,12 +196,12 @@ int admit(tn_server *s) {
     d.trunc_mode = p.r.trunc.mode;
     d.chi_max = int(std::min<uint32_t>(p.r.trunc.chi_max, 0x7fffffff));
     d.cutoff = p.r.trunc.cutoff;
-    if (int st = batch_bind(s->b, slot, d)) {
+    if (int st = batch_bind(c.b, slot, d)) {
       s->alloc.release(off, bytes);
-      s->free_slots.push_back(slot);
+      c.free_slots.push_back(slot);
       return st;
     }
-    Active &a = s->act[slot];
+    Active &a = c.act[slot];
     a.on = true;
     a.id = p.id;
     a.r = p.r;
@@ -164,52 +212,164 @@ int admit(tn_server *s) {
     a.bytes = bytes;
     a.entropy = 0;
     s->admitted += 1;
-    s->pending.pop_front();
+    c.active += 1;
+    c.pending.erase(c.pending.begin() + std::ptrdiff_t(pi));
   }
   return TN_OK;
+}
+
+// Admits what fits, generates the next layer of every active request of the
+// class and enqueues it (outputs are collected by collect()).
+int launch(tn_server *s, Class &c) {
+  if (int st = admit(s, c)) return st;
+  c.trajs.clear();
+  c.goff.assign(1, 0);
+  c.moff.assign(1, 0);
+  c.gks.clear();
+  c.mks.clear();
+  c.gates.clear();
+  c.us.clear();
+  for (uint32_t i = 0; i < uint32_t(c.act.size()); ++i) {
+    Active &a = c.act[i];
+    if (!a.on) continue;
+    const uint32_t n = a.r.n;
+    if (c.gk.size() < n) {
+      c.gk.resize(n);
+      c.mk.resize(n);
+      c.u.resize(n);
+      c.g.resize(32 * (n / 2 + 1));
+    }
+    uint32_t ng = 0, nm = 0;
+    if (int st = tn_gen_layer(a.r.seed, a.r.traj, a.layer, n, a.r.p, c.gk.data(), c.g.data(), &ng, c.mk.data(),
+                              c.u.data(), &nm))
+      return st;
+    c.trajs.push_back(i);
+    c.gks.insert(c.gks.end(), c.gk.begin(), c.gk.begin() + ng);
+    c.gates.insert(c.gates.end(), c.g.begin(), c.g.begin() + 32 * size_t(ng));
+    c.mks.insert(c.mks.end(), c.mk.begin(), c.mk.begin() + nm);
+    c.us.insert(c.us.end(), c.u.begin(), c.u.begin() + nm);
+    c.goff.push_back(uint32_t(c.gks.size()));
+    c.moff.push_back(uint32_t(c.mks.size()));
+  }
+  const uint32_t nt = uint32_t(c.trajs.size());
+  if (!nt) return TN_OK;
+  const double z = 0;
+  const uint32_t zu = 0;
+  if (int st = tn_batch_step(c.b, c.trajs.data(), nt, c.goff.data(), c.gks.empty() ? &zu : c.gks.data(),
+                             c.gates.empty() ? &z : c.gates.data(), c.moff.data(), c.mks.empty() ? &zu : c.mks.data(),
+                             c.us.empty() ? &z : c.us.data(), nullptr, nullptr, nullptr))
+    return st;
+  c.inflight = true;
+  c.launches += 1;
+  return TN_OK;
+}
+
+// Reads the entropies of the finished layer and retires completed requests.
+int collect(tn_server *s, Class &c, uint32_t *ndone) {
+  const uint32_t nt = uint32_t(c.trajs.size());
+  c.ents.resize(std::max<uint32_t>(nt, 1));
+  if (int st = batch_step_collect(c.b, nullptr, nullptr, c.ents.data())) return st;
+  c.inflight = false;
+  const double t_end = s->now();
+  for (uint32_t j = 0; j < nt; ++j) {
+    Active &a = c.act[c.trajs[j]];
+    a.entropy = c.ents[j];
+    a.layer += 1;
+    if (a.layer >= a.r.depth) {
+      tn_result res{};
+      res.id = a.id;
+      res.layers = a.layer;
+      res.final_entropy = a.entropy;
+      res.latency_s = t_end - a.t_arrival;
+      res.queue_s = a.t_admit - a.t_arrival;
+      res.status = 0;
+      s->done.push_back(res);
+      s->alloc.release(a.off, a.bytes);
+      a.on = false;
+      c.active -= 1;
+      c.free_slots.push_back(c.trajs[j]);
+      s->completed += 1;
+      ++*ndone;
+    }
+  }
+  c.layers += nt;
+  s->layers_done += nt;
+  c.trajs.clear();
+  return TN_OK;
+}
+
+uint32_t n_active(const tn_server *s) {
+  uint32_t k = 0;
+  for (int i = 0; i < s->ncls; ++i)
+    for (const auto &a : s->cls[i].act) k += a.on ? 1 : 0;
+  return k;
 }
 
 }  // namespace
 
 extern "C" {
 
-int tn_server_create(uint64_t hbm_bytes, uint32_t max_slots, int32_t precision, uint32_t max_chi, uint32_t max_n,
-                     tn_server **out) {
+int tn_server_create_classes(uint64_t hbm_bytes, uint32_t max_slots, int32_t precision, uint32_t max_chi,
+                             uint32_t max_n, uint32_t light_chi, uint32_t light_ctas, tn_server **out) {
   if (!out || hbm_bytes == 0 || max_slots == 0 || max_chi == 0 || max_n == 0) return TN_ERR_INVALID_ARG;
   if (precision != TN_PREC_F64 && precision != TN_PREC_MIXED) return TN_ERR_INVALID_ARG;
   *out = nullptr;
-  int cnt = 0;
+  int cnt = 0, dev = 0, sms = 1;
   if (cudaGetDeviceCount(&cnt) != cudaSuccess || cnt == 0) return TN_ERR_NO_DEVICE;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   tn_server *s = new tn_server();
   s->prec = precision;
   s->slots = max_slots;
   s->max_chi = max_chi;
   s->max_n = max_n;
-  int st = TN_OK;
-  s->b = batch_engine_create(max_slots, precision, int(max_chi), int(max_n), 0, &st);
-  if (!s->b) {
-    delete s;
-    return st;
+  if (light_chi == 0) light_chi = 64;
+  if (light_ctas == 0) light_ctas = uint32_t(std::max(1, sms / 5));
+  const bool two = light_chi < max_chi && int(light_ctas) < sms;
+  s->ncls = two ? 2 : 1;
+  s->cls[0].cap_max = two ? light_chi : max_chi;
+  s->cls[0].ctas = two ? int(light_ctas) : 0;
+  if (two) {
+    s->cls[1].cap_max = max_chi;
+    s->cls[1].ctas = sms - int(light_ctas);
+  }
+  for (int i = 0; i < s->ncls; ++i) {
+    Class &c = s->cls[i];
+    int st = TN_OK;
+    c.b = batch_engine_create(max_slots, precision, int(c.cap_max), int(max_n), c.ctas, &st);
+    if (!c.b) {
+      tn_server_free(s);
+      return st;
+    }
+    c.act.assign(max_slots, Active{});
+    for (uint32_t k = 0; k < max_slots; ++k) c.free_slots.push_back(max_slots - 1 - k);
   }
   cudaError_t e = cudaMalloc(&s->arena, size_t(hbm_bytes));
   if (e != cudaSuccess) {
-    tn_batch_free(s->b);
-    delete s;
+    s->arena = nullptr;
+    tn_server_free(s);
     set_last_error("cudaMalloc(serving arena)", e);
     return TN_ERR_OOM;
   }
   s->arena_bytes = size_t(hbm_bytes);
   s->alloc.init(s->arena_bytes);
-  s->act.assign(max_slots, Active{});
-  for (uint32_t i = 0; i < max_slots; ++i) s->free_slots.push_back(max_slots - 1 - i);
   s->t0 = std::chrono::steady_clock::now();
   *out = s;
   return TN_OK;
 }
 
+int tn_server_create(uint64_t hbm_bytes, uint32_t max_slots, int32_t precision, uint32_t max_chi, uint32_t max_n,
+                     tn_server **out) {
+  return tn_server_create_classes(hbm_bytes, max_slots, precision, max_chi, max_n, 0, 0, out);
+}
+
 int tn_server_free(tn_server *s) {
   if (!s) return TN_OK;
-  if (s->b) tn_batch_free(s->b);
+  for (int i = 0; i < 2; ++i) {
+    Class &c = s->cls[i];
+    if (c.b && c.inflight) batch_step_collect(c.b, nullptr, nullptr, nullptr);
+    if (c.b) tn_batch_free(c.b);
+  }
   if (s->arena) cudaFree(s->arena);
   delete s;
   return TN_OK;
@@ -229,83 +389,38 @@ int tn_server_submit(tn_server *s, const tn_request *r, double arrival, uint64_t
   if (footprint(s, *r, cap_of(*r)) > s->arena_bytes) return TN_ERR_CAPACITY;
   Pending p{s->next_id++, *r, arrival < 0 ? s->now() : arrival};
   if (id) *id = p.id;
-  s->pending.push_back(p);
+  s->cls[class_of(s, *r)].pending.push_back(p);
   return TN_OK;
 }
 
-int tn_server_tick(tn_server *s, uint32_t *n_active, uint32_t *n_done) {
+int tn_server_tick(tn_server *s, uint32_t *n_active_out, uint32_t *n_done) {
   if (!s) return TN_ERR_INVALID_ARG;
   const double t_start = s->now();
-  if (int st = admit(s)) return st;
-  s->trajs.clear();
-  s->goff.assign(1, 0);
-  s->moff.assign(1, 0);
-  s->gks.clear();
-  s->mks.clear();
-  s->gates.clear();
-  s->us.clear();
-  std::vector<uint32_t> gk(256), mk(256);
-  std::vector<double> g(32 * 128), u(256);
-  for (uint32_t i = 0; i < s->slots; ++i) {
-    Active &a = s->act[i];
-    if (!a.on) continue;
-    const uint32_t n = a.r.n;
-    if (gk.size() < n) {
-      gk.resize(n);
-      mk.resize(n);
-      u.resize(n);
-      g.resize(32 * (n / 2 + 1));
-    }
-    uint32_t ng = 0, nm = 0;
-    if (int st = tn_gen_layer(a.r.seed, a.r.traj, a.layer, n, a.r.p, gk.data(), g.data(), &ng, mk.data(), u.data(), &nm))
-      return st;
-    s->trajs.push_back(i);
-    s->gks.insert(s->gks.end(), gk.begin(), gk.begin() + ng);
-    s->gates.insert(s->gates.end(), g.begin(), g.begin() + 32 * size_t(ng));
-    s->mks.insert(s->mks.end(), mk.begin(), mk.begin() + nm);
-    s->us.insert(s->us.end(), u.begin(), u.begin() + nm);
-    s->goff.push_back(uint32_t(s->gks.size()));
-    s->moff.push_back(uint32_t(s->mks.size()));
-  }
-  const uint32_t nt = uint32_t(s->trajs.size());
   uint32_t ndone = 0;
-  if (nt) {
-    s->outc.resize(std::max<size_t>(1, s->mks.size()));
-    s->probs.resize(std::max<size_t>(1, s->mks.size()));
-    s->ents.resize(nt);
-    const double z = 0;
-    const uint32_t zu = 0;
-    if (int st = tn_batch_step(s->b, s->trajs.data(), nt, s->goff.data(), s->gks.empty() ? &zu : s->gks.data(),
-                               s->gates.empty() ? &z : s->gates.data(), s->moff.data(),
-                               s->mks.empty() ? &zu : s->mks.data(), s->us.empty() ? &z : s->us.data(),
-                               s->outc.data(), s->probs.data(), s->ents.data()))
-      return st;
-    const double t_end = s->now();
-    for (uint32_t j = 0; j < nt; ++j) {
-      Active &a = s->act[s->trajs[j]];
-      a.entropy = s->ents[j];
-      a.layer += 1;
-      if (a.layer >= a.r.depth) {
-        tn_result res{};
-        res.id = a.id;
-        res.layers = a.layer;
-        res.final_entropy = a.entropy;
-        res.latency_s = t_end - a.t_arrival;
-        res.queue_s = a.t_admit - a.t_arrival;
-        res.status = 0;
-        s->done.push_back(res);
-        s->alloc.release(a.off, a.bytes);
-        a.on = false;
-        s->free_slots.push_back(s->trajs[j]);
-        s->completed += 1;
-        ++ndone;
+  bool progress = false;
+  for (;;) {
+    bool any = false;
+    for (int i = 0; i < s->ncls; ++i) {
+      Class &c = s->cls[i];
+      if (c.inflight && batch_step_done(c.b)) {
+        if (int st = collect(s, c, &ndone)) return st;
+        progress = true;
       }
     }
-    s->layers_done += nt;
-    s->busy_s += t_end - t_start;
+    for (int i = 0; i < s->ncls; ++i) {
+      Class &c = s->cls[i];
+      if (!c.inflight)
+        if (int st = launch(s, c)) return st;
+      any = any || c.inflight;
+    }
+    if (progress || !any) break;
+    std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+  if (progress) {
+    s->busy_s += s->now() - t_start;
     s->ticks += 1;
   }
-  if (n_active) *n_active = nt;
+  if (n_active_out) *n_active_out = n_active(s);
   if (n_done) *n_done = ndone;
   return TN_OK;
 }
@@ -323,16 +438,40 @@ int tn_server_poll(tn_server *s, tn_result *out, uint32_t cap, uint32_t *n) {
 
 int tn_server_stats(const tn_server *s, double *out) {
   if (!s || !out) return TN_ERR_INVALID_ARG;
-  uint32_t active = 0;
-  for (const auto &a : s->act) active += a.on ? 1 : 0;
+  size_t pending = 0;
+  for (int i = 0; i < s->ncls; ++i) pending += s->cls[i].pending.size();
   out[0] = s->layers_done;
   out[1] = s->busy_s;
   out[2] = s->ticks;
   out[3] = double(s->alloc.used());
-  out[4] = double(s->pending.size());
-  out[5] = double(active);
+  out[4] = double(pending);
+  out[5] = double(n_active(s));
   out[6] = s->admitted;
   out[7] = s->completed;
+  return TN_OK;
+}
+
+int tn_server_set_policy(tn_server *s, int32_t policy, uint32_t max_active0, uint32_t max_active1) {
+  if (!s || policy < 0 || policy > 1) return TN_ERR_INVALID_ARG;
+  s->policy = policy;
+  s->cls[0].max_active = max_active0;
+  s->cls[1].max_active = max_active1;
+  return TN_OK;
+}
+
+int tn_server_class_stats(const tn_server *s, uint32_t cls, double *out) {
+  if (!s || !out || cls >= 2) return TN_ERR_INVALID_ARG;
+  for (int i = 0; i < 6; ++i) out[i] = 0;
+  if (int(cls) >= s->ncls) return TN_OK;
+  const Class &c = s->cls[cls];
+  uint32_t active = 0;
+  for (const auto &a : c.act) active += a.on ? 1 : 0;
+  out[0] = double(c.cap_max);
+  out[1] = double(c.ctas);
+  out[2] = c.layers;
+  out[3] = c.launches;
+  out[4] = double(c.pending.size());
+  out[5] = double(active);
   return TN_OK;
 }
 

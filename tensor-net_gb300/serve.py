@@ -15,12 +15,17 @@ from .mps import PRECISIONS, Trunc
 
 
 class Server:
+    """Requests with bond capacity <= light_chi run in class 0 on light_ctas
+    CTAs, the rest in class 1 on the remaining SMs; the classes step
+    independently (0 = defaults: 64 and a fifth of the SMs)."""
+
     def __init__(self, hbm_bytes: int, max_slots: int = 1024, precision: str = "mixed", max_chi: int = 512,
-                 max_n: int = 128):
+                 max_n: int = 128, light_chi: int = 0, light_ctas: int = 0):
         self._lib = L.lib()
         self._h = C.c_void_p()
-        L.check(self._lib.tn_server_create(int(hbm_bytes), int(max_slots), PRECISIONS[precision], int(max_chi),
-                                           int(max_n), C.byref(self._h)), "tn_server_create")
+        L.check(self._lib.tn_server_create_classes(int(hbm_bytes), int(max_slots), PRECISIONS[precision],
+                                                   int(max_chi), int(max_n), int(light_chi), int(light_ctas),
+                                                   C.byref(self._h)), "tn_server_create_classes")
 
     def close(self):
         if self._h:
@@ -61,6 +66,18 @@ class Server:
         L.check(self._lib.tn_server_stats(self._h, L.dptr(out)), "tn_server_stats")
         return dict(layers=out[0], busy_s=out[1], ticks=out[2], arena_used=out[3], pending=out[4], active=out[5],
                     admitted=out[6], completed=out[7])
+
+    def set_policy(self, policy: str = "fcfs", max_active=(0, 0)):
+        """Admission order within a class ("fcfs" or "least-work") and the
+        cap on resident requests per class (0 = every slot)."""
+        L.check(self._lib.tn_server_set_policy(self._h, {"fcfs": 0, "least-work": 1}[policy], int(max_active[0]),
+                                               int(max_active[1])), "tn_server_set_policy")
+
+    def class_stats(self, cls: int):
+        out = np.zeros(6)
+        L.check(self._lib.tn_server_class_stats(self._h, int(cls), L.dptr(out)), "tn_server_class_stats")
+        return dict(cap_max=int(out[0]), ctas=int(out[1]), layers=out[2], launches=out[3], pending=int(out[4]),
+                    active=int(out[5]))
 
 
 def poisson_requests(rate, duration, seed, n_range=(16, 128), chis=(64, 128, 256, 512), p_range=(0.02, 0.3),

@@ -222,3 +222,31 @@ def test_batch_matches_single_and_is_mix_independent(pkg, ref):
         assert abs(ents[1] - rtraj.entropy_vn(ns[1] // 2 - 1)) < 1e-9
     np.testing.assert_array_equal(mix.svals(1, 4), alone.svals(0, 4))
     assert mix.device_status() == 0
+
+
+def test_batch_schedules_agree(pkg):
+    """The one-launch schedule (sweep items pushed as a trajectory's gates
+    finish) and the two-launch schedule give bit-identical results, including
+    trajectories with no gate in a layer (n = 2 on odd layers, n = 3 rows
+    where the brickwork leaves one gate) whose sweep items are pushed before
+    the launch."""
+    specs = [(2, 4, 0.3), (12, 16, 0.2), (3, 4, 0.5), (9, 32, 0.25), (16, 32, 0.1), (5, 8, 0.0)]
+    ns = [s[0] for s in specs]
+    truncs = [pkg.Trunc.both(s[1], 1e-12) for s in specs]
+    one = pkg.Batch(ns, truncs, "mixed")
+    two = pkg.Batch(ns, truncs, "mixed")
+    one.set_schedule(1)
+    two.set_schedule(0)
+    order = list(range(len(specs)))
+    for t in range(10):
+        layers = [pkg.gen_layer(31, i, t, s[0], s[2]) for i, s in enumerate(specs)]
+        r1, e1 = one.step(order, layers)
+        r0, e0 = two.step(order, layers)
+        assert r1 == r0
+        assert list(e1) == list(e0)
+        ms1, ms0 = one.last_launch_ms(), two.last_launch_ms()
+        assert ms1[1] == 0.0 and ms0[1] > 0.0
+    for i in range(len(specs)):
+        for bnd in range(ns[i] - 1):
+            np.testing.assert_array_equal(one.svals(i, bnd), two.svals(i, bnd))
+    assert one.device_status() == 0 and two.device_status() == 0

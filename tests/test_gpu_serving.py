@@ -14,8 +14,9 @@ def _req_params():
             dict(n=14, chi=16, p=0.15, depth=5, traj=4), dict(n=10, chi=32, p=0.2, depth=12, traj=5)]
 
 
-def _run(pkg, reqs, slots, hbm, stagger):
-    s = pkg.Server(hbm, max_slots=slots, precision="mixed", max_chi=32, max_n=16)
+def _run(pkg, reqs, slots, hbm, stagger, light_chi=0, light_ctas=0, class_stats=False):
+    s = pkg.Server(hbm, max_slots=slots, precision="mixed", max_chi=32, max_n=16, light_chi=light_chi,
+                   light_ctas=light_ctas)
     ids = {}
     pending = list(reqs)
     results = {}
@@ -31,6 +32,8 @@ def _run(pkg, reqs, slots, hbm, stagger):
         ticks += 1
         assert ticks < 500
     st = s.stats()
+    if class_stats:
+        st["classes"] = [s.class_stats(0), s.class_stats(1)]
     s.close()
     return results, st
 
@@ -44,6 +47,22 @@ def test_results_same_alone_and_in_the_mix(pkg):
         a, m = alone[r["traj"]], mix[r["traj"]]
         assert a["layers"] == m["layers"] == r["depth"]
         assert a["final_entropy"] == m["final_entropy"], (r, a, m)
+
+
+def test_two_classes_step_independently(pkg):
+    # bond capacity <= 16 -> class 0 on 8 CTAs, 32 -> class 1 on the other SMs
+    reqs = _req_params()
+    mix, st = _run(pkg, reqs, slots=4, hbm=1 << 30, stagger=1, light_chi=16, light_ctas=8, class_stats=True)
+    assert st["completed"] == len(reqs) and st["active"] == 0 and st["arena_used"] == 0
+    c0, c1 = st["classes"]
+    assert (c0["cap_max"], c0["ctas"], c1["cap_max"]) == (16, 8, 32)
+    light = [r for r in reqs if min(r["chi"], 1 << (r["n"] // 2)) <= 16]
+    heavy = [r for r in reqs if r not in light]
+    assert c0["layers"] == sum(r["depth"] for r in light) and c1["layers"] == sum(r["depth"] for r in heavy)
+    # the same request gives the same bits in either class layout and alone
+    one, _ = _run(pkg, reqs, slots=4, hbm=1 << 30, stagger=1)
+    for r in reqs:
+        assert mix[r["traj"]]["final_entropy"] == one[r["traj"]]["final_entropy"], r
 
 
 def test_admission_waits_for_memory(pkg):
@@ -65,3 +84,30 @@ def test_admission_waits_for_memory(pkg):
     assert done[1]["queue_s"] > 0.0
     with pytest.raises(pkg.TnError):
         s.submit(64, pkg.Trunc.both(32, 1e-10), 0.1, 4, 5, 2)  # n beyond max_n
+
+
+def test_least_work_policy_and_active_cap(pkg):
+    # one resident request at a time: the cheaper request, submitted second,
+    # is admitted first under the least-work policy, and its result is the
+    # same as under first come, first served
+    out = {}
+    for policy in ("fcfs", "least-work"):
+        s = pkg.Server(1 << 30, max_slots=4, precision="mixed", max_chi=32, max_n=16)
+        s.set_policy(policy, (1, 0))
+        big = s.submit(14, pkg.Trunc.both(32, 1e-10), 0.1, 6, 3, 0)
+        small = s.submit(8, pkg.Trunc.both(8, 1e-10), 0.1, 3, 3, 1)
+        order = []
+        res = {}
+        for _ in range(40):
+            a, _ = s.tick()
+            assert a <= 1
+            for d in s.poll():
+                order.append(d["id"])
+                res[d["id"]] = d
+            if len(order) == 2:
+                break
+        s.close()
+        assert sorted(order) == sorted([big, small])
+        out[policy] = (order, res[big]["final_entropy"], res[small]["final_entropy"])
+    assert out["fcfs"][0][0] == 1 and out["least-work"][0][0] == 2
+    assert out["fcfs"][1:] == out["least-work"][1:]
