@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--schedule", type=int, default=1, choices=[0, 1])
+    ap.add_argument("--workload", default="batch", choices=["batch", "mixed", "large"],
+                    help="batch: the headline line; mixed: the batching workload; large: n=128, chi_max=1024")
+    ap.add_argument("--large-seconds", type=float, default=300.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=60.0)
@@ -246,6 +249,10 @@ def cpu_baseline(n, chi, cutoff, layers_by_traj, budget, cores=None):
 
 
 # --------------------------------------------------------------- GPU arm
+# per-phase SM cycles of the bond operations, counted on the device (one CTA each)
+CYC_KEYS = ("cyc_theta", "cyc_gram", "cyc_rot", "cyc_update", "cyc_final")
+
+
 def run_gpu(a, rank, world, local_rank):
     import numpy as np
     import torch
@@ -275,12 +282,9 @@ def run_gpu(a, rank, world, local_rank):
     # stage W + K layers of inputs in HBM
     dev = torch.device("cuda", local_rank)
     staged = []
-    order = None
     for t in range(a.prefill, a.prefill + a.warmup + a.steps):
         pk = batch.pack(trajs, layer_inputs(t))
         nm = int(pk["meas_off"][-1])
-        if order is None:
-            order = torch.arange(B, dtype=torch.int32, device=dev)
         staged.append(dict(
             trajs=torch.as_tensor(pk["trajs"].astype(np.int32), device=dev),
             gate_off=torch.as_tensor(pk["gate_off"].astype(np.int32), device=dev),
@@ -296,7 +300,7 @@ def run_gpu(a, rank, world, local_rank):
     stream = torch.cuda.ExternalStream(batch.stream(), device=dev)
 
     def launch(s):
-        batch.step_ptrs(B, s["trajs"].data_ptr(), order.data_ptr(), s["gate_off"].data_ptr(),
+        batch.step_ptrs(B, s["trajs"].data_ptr(), None, s["gate_off"].data_ptr(),
                         s["gate_ks"].data_ptr(), s["gates"].data_ptr(), s["meas_off"].data_ptr(),
                         s["meas_ks"].data_ptr(), s["us"].data_ptr(), s["outc"].data_ptr(),
                         s["probs"].data_ptr(), s["ents"].data_ptr())
@@ -425,6 +429,116 @@ def run_serving(a, pkg):
                     "exceeds capacity: most heavy requests are still running or queued when it closes)"}
 
 
+def _dev_view(torch, ptr, n, typestr):
+    class V:
+        __cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False), "version": 2}
+    return torch.as_tensor(V(), device="cuda")
+
+
+def run_mixed(a):
+    """The batching workload: `--batch` trajectories with n uniform in
+    {16, 32, 48, 64}, chi_max uniform in {32, 64, 128, 256}, p uniform in
+    [0.05, 0.3], per-trajectory seeds (depth 4n >= 64 layers, so every
+    trajectory is live in the window); one graph-captured launch per layer
+    (tn_batch_step_device) with the layer inputs copied device-to-device into
+    the graph's input buffers; `--prefill` untimed layers, then W + K."""
+    import numpy as np
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    rng = np.random.default_rng(a.seed)
+    B = a.batch
+    ns = rng.choice([16, 32, 48, 64], B)
+    chis = rng.choice([32, 64, 128, 256], B)
+    ps = rng.uniform(0.05, 0.3, B)
+    batch = pkg.Batch([int(x) for x in ns], [pkg.Trunc.both(int(c), a.cutoff) for c in chis], a.prec)
+    batch.set_schedule(a.schedule)
+    trajs = list(range(B))
+
+    def layer(t):
+        return [pkg.gen_layer(a.seed, i, t, int(ns[i]), float(ps[i])) for i in trajs]
+    assert a.prefill + a.warmup + a.steps <= 4 * 16, "every trajectory must still be live"
+    for t in range(a.prefill):
+        batch.step(trajs, layer(t))
+    ptr = batch.device_inputs(int(sum(ns // 2)), int(sum(ns)))
+    dev = torch.device("cuda")
+    staged = []
+    for t in range(a.prefill, a.prefill + a.warmup + a.steps):
+        pk = batch.pack(trajs, layer(t))
+        staged.append([(name, ts, torch.as_tensor(np.ascontiguousarray(pk[name].astype(dt)), device=dev))
+                       for name, ts, dt in (("trajs", "<i4", np.int32), ("gate_off", "<i4", np.int32),
+                                            ("gate_ks", "<i4", np.int32), ("gates", "<f8", np.float64),
+                                            ("meas_off", "<i4", np.int32), ("meas_ks", "<i4", np.int32),
+                                            ("us", "<f8", np.float64)) if pk[name].size])
+    stream = torch.cuda.ExternalStream(batch.stream(), device=dev)
+    views = {}
+
+    def run(layer_arrays):
+        for name, ts, src in layer_arrays:
+            key = (name, src.numel())
+            if key not in views:
+                views[key] = _dev_view(torch, ptr[name], src.numel(), ts)
+            views[key].copy_(src, non_blocking=True)
+        batch.step_device(B)
+    with torch.cuda.stream(stream):
+        for L_ in staged[: a.warmup]:
+            run(L_)
+    batch.synchronize()
+    batch.stats(reset=True)
+    clocks = ClockSampler(0)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        ev0.record(stream)
+        for L_ in staged[a.warmup:]:
+            run(L_)
+        ev1.record(stream)
+    batch.synchronize()
+    clk = clocks.stop()
+    elapsed = ev0.elapsed_time(ev1) / 1e3
+    st = batch.stats(reset=True)
+    status = batch.device_status()
+    return {"workload": "batching: n in {16,32,48,64}, chi_max in {32,64,128,256}, p in U[0.05,0.3], "
+                        "per-trajectory seeds, one graph-captured launch per layer",
+            "trajectories": B, "value": B * a.steps / elapsed, "unit": UNIT, "ms_per_step": elapsed / a.steps * 1e3,
+            "layers": [a.prefill + a.warmup, a.prefill + a.warmup + a.steps],
+            "tflops_algorithmic": (st["flop_theta"] + st["flop_svd"]) / elapsed / 1e12,
+            "bond_ops_per_step": st["bond_ops"] / a.steps, "device_status": status, "clocks": clk,
+            "precision": a.prec}
+
+
+def run_large(a):
+    """The large single trajectory: n=128, chi_max=1024, p=0.05, cutoff 1e-10,
+    layers from |0...0> until `--large-seconds` of wall time; entropy and
+    wall time per layer (one trajectory of a batch, one launch per layer)."""
+    import numpy as np
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    n, chi, p = 128, 1024, 0.05
+    batch = pkg.Batch([n], [pkg.Trunc.both(chi, a.cutoff)], a.prec)
+    batch.set_schedule(a.schedule)
+    rows = []
+    t_start = time.perf_counter()
+    t = 0
+    while time.perf_counter() - t_start < a.large_seconds and t < 256:
+        inputs = [pkg.gen_layer(a.seed, 0, t, n, p)]
+        batch.stats(reset=True)
+        t0 = time.perf_counter()
+        _, ent = batch.step([0], inputs)
+        dt = time.perf_counter() - t0
+        st = batch.stats(reset=True)
+        dims = batch.bond_dims(0)
+        rows.append({"layer": t, "s": dt, "entropy": float(ent[0]), "max_bond": int(dims.max()),
+                     "tflops_algorithmic": (st["flop_theta"] + st["flop_svd"]) / dt / 1e12,
+                     "bond_ops": int(st["bond_ops"])})
+        t += 1
+    torch.cuda.synchronize()
+    return {"workload": f"single trajectory n={n} chi_max={chi} p={p} cutoff={a.cutoff:g} from |0...0>",
+            "layers_run": t, "precision": a.prec, "per_layer": rows, "device_status": batch.device_status(),
+            "unit": "s per layer"}
+
+
 def main():
     a = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -463,6 +577,17 @@ def main():
         print(json.dumps(out), flush=True)
         return
 
+    if a.workload in ("mixed", "large"):
+        if rank != 0:
+            return
+        import torch
+        torch.cuda.set_device(0)
+        out = run_mixed(a) if a.workload == "mixed" else run_large(a)
+        out.update({"metric": METRIC if a.workload == "mixed" else "per-layer time and entropy",
+                    "n_gpus": 1, "data": "synthetic (seeded Haar gates and measurement uniforms)"})
+        print(json.dumps(out), flush=True)
+        return
+
     import torch
     if world > 1:
         torch.distributed.init_process_group("nccl")
@@ -475,6 +600,7 @@ def main():
     peak = float(peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops"))
     tr = ncu_traffic()
     sm_mhz = r["clocks"].get("sm_mhz") or 2070.0
+    cyc_sum = sum(r["stats"][k] for k in CYC_KEYS)
     simt_peak = r["sms"] * 128 * 2 * sm_mhz * 1e6 / 1e12
     out = {
         "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps,
@@ -498,6 +624,8 @@ def main():
                               else "two launches per layer (gates, then sweeps)"),
                  "launch_ms (gate+sweep launch | gate launch, sweep launch)": r["split"],
                  "lq_refactors_per_step": r["stats"]["lq_ops"] / a.steps,
+                 "bond_op_cycle_share": {k[4:]: r["stats"][k] / cyc_sum for k in CYC_KEYS} if cyc_sum else None,
+                 "ctas_busy_in_bond_ops": (cyc_sum / (r["sms"] * sm_mhz * 1e6 * r["elapsed"])) if cyc_sum else None,
                  "svd_sweep_limit_hits": [r["stats"]["nonconv"], r["stats"]["nonconv_c_lq"],
                                           r["stats"]["nonconv_c_direct"]],
                  "device_status": r["status"], "middle_bond_dims": [int(d[a.n // 2 - 1]) for d in r["dims"]]},

@@ -223,7 +223,8 @@ int tn_batch_device_inputs(tn_batch *b, uint32_t max_gates, uint32_t max_meas,
 int tn_batch_step_device(tn_batch *b, uint32_t nt);
 /* Same layer with every array supplied by the caller in device memory
  * (int32 indices, float64 gates/uniforms): trajs[nt], order[nt] (execution
- * rank of each entry: a permutation of 0..nt-1, 0 runs first), gate_off[nt+1],
+ * rank of each entry: a permutation of 0..nt-1, 0 runs first; NULL = most
+ * expensive first by the current bond dimensions, ranked on the device), gate_off[nt+1],
  * gate_ks[], gates[32 per gate], meas_off[nt+1], meas_ks[], us[], and outputs
  * outcomes[], probs[], entropy[nt].  Stream-ordered on the batch stream, no
  * synchronisation, no host copies. */

@@ -121,6 +121,22 @@ class Batch:
         L.check(self._lib.tn_batch_step_ptrs(self._h, int(nt), trajs, order, gate_off, gate_ks, gates, meas_off,
                                              meas_ks, us, outcomes, probs, entropy), "tn_batch_step_ptrs")
 
+    _INPUT_NAMES = ("trajs", "gate_off", "gate_ks", "gates", "meas_off", "meas_ks", "us", "outcomes", "probs",
+                    "entropy")
+
+    def device_inputs(self, max_gates: int, max_meas: int):
+        """Device buffers of the graph-captured step (tn_batch_device_inputs):
+        name -> device pointer (int32 indices, float64 gates/uniforms)."""
+        ptrs = [C.c_void_p() for _ in self._INPUT_NAMES]
+        L.check(self._lib.tn_batch_device_inputs(self._h, int(max_gates), int(max_meas),
+                                                 *[C.byref(p) for p in ptrs]), "tn_batch_device_inputs")
+        return {k: int(p.value) for k, p in zip(self._INPUT_NAMES, ptrs)}
+
+    def step_device(self, nt: int):
+        """Replay the captured layer launch for the first nt listed trajectories
+        (stream-ordered on the batch stream, no synchronisation)."""
+        L.check(self._lib.tn_batch_step_device(self._h, int(nt)), "tn_batch_step_device")
+
     def slot_bytes(self, t: int) -> int:
         b = L.u64()
         L.check(self._lib.tn_batch_slot_bytes(self._h, int(t), C.byref(b)), "slot_bytes")

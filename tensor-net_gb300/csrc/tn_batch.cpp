@@ -75,7 +75,7 @@ struct tn_batch {
   // [8] push counter, [9] queue-wait error
   int *dcounter = nullptr;
   int schedule = 1;  // 1: one launch per layer, sweeps pushed as gates finish; 0: two launches
-  int *drem = nullptr, *dgstart = nullptr, *dscratch = nullptr;
+  int *drem = nullptr, *dgstart = nullptr, *dscratch = nullptr, *dorder = nullptr;
   Item *ddyn = nullptr;
   // device-input mode
   void *din = nullptr;
@@ -141,7 +141,7 @@ int ensure_step(tn_batch *b, uint32_t nt, uint32_t ng, uint32_t nm) {
   const size_t nbytes = sizeof(int) * NT;
   CKB(cudaMalloc(reinterpret_cast<void **>(&b->dprog),
                  align256(pbytes) + 2 * align256(ibytes) + align256(gpbytes) + align256(gibytes) +
-                     3 * align256(nbytes) + 256));
+                     4 * align256(nbytes) + 256));
   char *base = reinterpret_cast<char *>(b->dprog);
   size_t at = align256(pbytes);
   auto take = [&](size_t bytes) {
@@ -156,6 +156,7 @@ int ensure_step(tn_batch *b, uint32_t nt, uint32_t ng, uint32_t nm) {
   b->drem = reinterpret_cast<int *>(take(nbytes));
   b->dgstart = reinterpret_cast<int *>(take(nbytes));
   b->dscratch = reinterpret_cast<int *>(take(nbytes));
+  b->dorder = reinterpret_cast<int *>(take(nbytes));
   b->step_nt = NT;
   b->step_ng = NG;
   b->step_nm = NM;
@@ -186,7 +187,12 @@ StepPtrs ptrs_of(const StepLayout &L, char *dbase) {
   return p;
 }
 
-int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P, bool timed = true) {
+int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P0, bool timed = true) {
+  StepPtrs P = P0;
+  if (!P.order) {  // most expensive trajectories first, by their current bond dimensions
+    CKB(launch_lpt_order(b->dtraj, P.list, int(nt), P.moff, b->dorder, b->st));
+    P.order = b->dorder;
+  }
   LaunchArgs la{};
   la.trajs = b->dtraj;
   la.gates = P.gates;
@@ -448,17 +454,6 @@ int tn_batch_step(tn_batch *b, const uint32_t *trajs, uint32_t nt, const uint32_
   if (int s = ensure_step(b, nt, ng, nm)) return s;
   StepLayout L = step_layout(b->step_nt, b->step_ng, b->step_nm);
   char *hb = reinterpret_cast<char *>(b->hstep);
-  // most expensive first: cost ~ program length * chi^3
-  std::vector<std::pair<double, uint32_t>> cost(nt);
-  for (uint32_t i = 0; i < nt; ++i) {
-    const TrajDev &d = b->h[trajs[i]];
-    double c = std::min<double>(d.cap, double(max_rank(uint32_t(d.n))));
-    double ops = double(gate_off[i + 1] - gate_off[i]) + (meas_off[i + 1] > meas_off[i] ? 2.0 * d.n : 0.0) + 1.0;
-    cost[i] = {-(ops * c * c * c), i};
-  }
-  std::stable_sort(cost.begin(), cost.end());
-  int *ord = reinterpret_cast<int *>(hb + L.order);
-  for (uint32_t r = 0; r < nt; ++r) ord[cost[r].second] = int(r);
   int *lst = reinterpret_cast<int *>(hb + L.list);
   int *go = reinterpret_cast<int *>(hb + L.goff);
   int *mo = reinterpret_cast<int *>(hb + L.moff);
@@ -474,7 +469,9 @@ int tn_batch_step(tn_batch *b, const uint32_t *trajs, uint32_t nt, const uint32_
   if (ng) std::memcpy(hb + L.gates, gates, sizeof(double) * 32 * ng);
   if (nm) std::memcpy(hb + L.us, us, sizeof(double) * nm);
   CKB(cudaMemcpyAsync(b->dstep, b->hstep, L.in_bytes, cudaMemcpyHostToDevice, b->st));
-  if (int s = launch_step(b, nt, ptrs_of(L, reinterpret_cast<char *>(b->dstep)))) return s;
+  StepPtrs P = ptrs_of(L, reinterpret_cast<char *>(b->dstep));
+  P.order = nullptr;  // ranked on the device from the current bond dimensions
+  if (int s = launch_step(b, nt, P)) return s;
   const size_t out_bytes = L.total - L.out_off;
   CKB(cudaMemcpyAsync(hb + L.out_off, reinterpret_cast<char *>(b->dstep) + L.out_off, out_bytes,
                       cudaMemcpyDeviceToHost, b->st));
@@ -501,10 +498,6 @@ int tn_batch_device_inputs(tn_batch *b, uint32_t max_gates, uint32_t max_meas, v
   b->din_gates = max_gates;
   b->din_meas = max_meas;
   char *d = reinterpret_cast<char *>(b->din);
-  // execution order = list order in this mode
-  std::vector<int> ident(b->ntraj);
-  std::iota(ident.begin(), ident.end(), 0);
-  CKB(cudaMemcpy(d + L.order, ident.data(), sizeof(int) * b->ntraj, cudaMemcpyHostToDevice));
   if (d_trajs) *d_trajs = d + L.list;
   if (d_gate_off) *d_gate_off = d + L.goff;
   if (d_gate_ks) *d_gate_ks = d + L.gks;
@@ -527,7 +520,9 @@ int tn_batch_step_device(tn_batch *b, uint32_t nt) {
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ge = nullptr;
     CKB(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
-    int s = launch_step(b, nt, ptrs_of(L, reinterpret_cast<char *>(b->din)), false);
+    StepPtrs P = ptrs_of(L, reinterpret_cast<char *>(b->din));
+    P.order = nullptr;  // ranked on the device inside the graph
+    int s = launch_step(b, nt, P, false);
     cudaError_t e = cudaStreamEndCapture(b->st, &g);
     if (s != TN_OK) {
       if (g) cudaGraphDestroy(g);
@@ -546,7 +541,7 @@ int tn_batch_step_device(tn_batch *b, uint32_t nt) {
 int tn_batch_step_ptrs(tn_batch *b, uint32_t nt, const void *d_trajs, const void *d_order, const void *d_gate_off,
                        const void *d_gate_ks, const void *d_gates, const void *d_meas_off, const void *d_meas_ks,
                        const void *d_us, void *d_outcomes, void *d_probs, void *d_entropy) {
-  if (!b || nt > b->ntraj || !d_trajs || !d_order || !d_gate_off || !d_meas_off || !d_entropy)
+  if (!b || nt > b->ntraj || !d_trajs || !d_gate_off || !d_meas_off || !d_entropy)
     return TN_ERR_INVALID_ARG;
   if (nt == 0) return TN_OK;
   if (int s = ensure_step(b, b->ntraj, 1, 1)) return s;

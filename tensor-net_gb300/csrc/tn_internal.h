@@ -116,6 +116,10 @@ cudaError_t launch_reset(TrajDev *trajs, const int *list, int count, int prec, c
 cudaError_t launch_compile(const TrajDev *trajs, const int *list, int nt, const int *order, const int *gate_off,
                            const int *gate_ks, const int *meas_off, const int *meas_ks, int pcap, Instr *prog,
                            Item *items, Instr *gprog, Item *gitems, int gcap, int *gcount, cudaStream_t st);
+// order[i] = execution rank of listed trajectory i, most expensive first by
+// the current bond dimensions (a single-block sort on the device).
+cudaError_t launch_lpt_order(const TrajDev *trajs, const int *list, int nt, const int *meas_off, int *order,
+                             cudaStream_t st);
 // Dependency-driven variant: gate items placed trajectory by trajectory in
 // `order` rank (gstart from a scan over ranks, scratch: nt ints), sweep
 // programs at sweeps[i], rem[i] = gate items of trajectory i, and trajectories

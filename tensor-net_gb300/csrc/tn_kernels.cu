@@ -176,6 +176,46 @@ __global__ void k_compile(const TrajDev *trajs, const int *list, int nt, const i
   items[order[i]] = Item{t, int(size_t(i) * pcap), pc, 0};
 }
 
+// Execution rank of every listed trajectory, most expensive first (one
+// block of 1024 threads).  Cost from the current bond dimensions: the
+// trajectory's critical path is its most expensive gate (gates run in
+// parallel) plus, when the layer measures, its serial refactor sweep over
+// every bond, each bond op ~ chi^3.  Ties keep list order; more than
+// kLptMax trajectories keep list order altogether.
+constexpr int kLptMax = 4096;
+
+__global__ void __launch_bounds__(1024) k_lpt_order(const TrajDev *trajs, const int *list, int nt,
+                                                    const int *meas_off, int *order) {
+  extern __shared__ __align__(16) unsigned char lsm[];
+  if (nt > kLptMax) {
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) order[i] = i;
+    return;
+  }
+  int P = 1;
+  while (P < nt) P <<= 1;
+  double *key = reinterpret_cast<double *>(lsm);
+  int *idx = reinterpret_cast<int *>(key + P);
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    double c = -1.0;
+    if (i < nt) {
+      const TrajDev tr = trajs[list[i]];
+      double sweep = 0.0, gmax = 0.0;
+      for (int b = 1; b < tr.n; ++b) {
+        const double x = double(tr.chi[b]);
+        const double x3 = x * x * x;
+        sweep += x3;
+        gmax = fmax(gmax, x3);
+      }
+      c = gmax + (meas_off[i + 1] > meas_off[i] ? sweep : 0.0);
+    }
+    key[i] = c;
+    idx[i] = i;
+  }
+  __syncthreads();
+  bitonic_desc<float, 1024, kBlockW>(key, idx, P);
+  for (int r = threadIdx.x; r < nt; r += blockDim.x) order[idx[r]] = r;
+}
+
 // First gate-queue slot of every listed trajectory when trajectories are
 // taken in `order` rank: an exclusive scan of the gate counts by rank (one
 // block; scratch holds the counts by rank).  An `order` that is not a
@@ -299,15 +339,28 @@ __global__ void k_compile_dd(const TrajDev *trajs, const int *list, int nt, cons
 }
 
 // ------------------------------------------------------------- launchers
+// Dynamic shared memory limit configured for k_run<T> on the current
+// device (raised on demand; set when a handle or batch is created, so that
+// a stream capture of a launch finds it already in place).
+template <typename T, int NT, int W>
+static cudaError_t ensure_run_smem(size_t smem) {
+  static int configured[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int &have = configured[dev & 63];
+  if (int(smem) > have) {
+    cudaError_t e = cudaFuncSetAttribute(k_run<T, NT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    have = int(smem);
+  }
+  return cudaSuccess;
+}
+
 template <typename T, int NT, int W>
 static cudaError_t launch_run_t(const LaunchArgs &la, int grid, int sortP, int ws_cap, cudaStream_t st) {
   const size_t smem = SmemLayout<T, W>::total(sortP);
-  static int configured_bytes = 0;
-  if (int(smem) > configured_bytes) {
-    cudaError_t e = cudaFuncSetAttribute(k_run<T, NT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e != cudaSuccess) return e;
-    configured_bytes = int(smem);
-  }
+  cudaError_t e = ensure_run_smem<T, NT, W>(smem);
+  if (e != cudaSuccess) return e;
   k_run<T, NT, W><<<grid, NT, smem, st>>>(la, sortP, ws_cap);
   return cudaGetLastError();
 }
@@ -329,10 +382,10 @@ int run_blocks_per_sm(int prec, int sortP) {
   const size_t smem = run_smem_bytes(prec, sortP);
   cudaError_t e;
   if (prec == 0) {
-    cudaFuncSetAttribute(k_run<double, kThreads, kBlockW>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    ensure_run_smem<double, kThreads, kBlockW>(smem);
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_run<double, kThreads, kBlockW>, kThreads, smem);
   } else {
-    cudaFuncSetAttribute(k_run<float, kThreads, kBlockW>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    ensure_run_smem<float, kThreads, kBlockW>(smem);
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_run<float, kThreads, kBlockW>, kThreads, smem);
   }
   if (e != cudaSuccess || nb < 1) nb = 1;
@@ -351,6 +404,15 @@ cudaError_t launch_compile(const TrajDev *trajs, const int *list, int nt, const 
   if (nt <= 0) return cudaSuccess;
   k_compile<<<(nt + 127) / 128, 128, 0, st>>>(trajs, list, nt, order, gate_off, gate_ks, meas_off, meas_ks, pcap,
                                               prog, items, gprog, gitems, gcap, gcount);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lpt_order(const TrajDev *trajs, const int *list, int nt, const int *meas_off, int *order,
+                             cudaStream_t st) {
+  if (nt <= 0) return cudaSuccess;
+  int P = 1;
+  while (P < nt && P < kLptMax) P <<= 1;
+  k_lpt_order<<<1, 1024, size_t(P) * (sizeof(double) + sizeof(int)), st>>>(trajs, list, nt, meas_off, order);
   return cudaGetLastError();
 }
 

@@ -250,3 +250,52 @@ def test_batch_schedules_agree(pkg):
         for bnd in range(ns[i] - 1):
             np.testing.assert_array_equal(one.svals(i, bnd), two.svals(i, bnd))
     assert one.device_status() == 0 and two.device_status() == 0
+
+
+class _DevView:
+    """A raw device range seen by torch through __cuda_array_interface__."""
+
+    def __init__(self, ptr, n, typestr):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False), "version": 2}
+
+
+def test_graph_captured_step_matches_host_step(pkg):
+    """tn_batch_step_device (a CUDA graph of the layer's scan, compile and
+    executor launch, captured once per trajectory count) gives the same bits
+    as tn_batch_step, including when the number of listed trajectories
+    changes between layers (a second capture)."""
+    torch = pytest.importorskip("torch")
+    specs = [(10, 16, 0.2), (7, 8, 0.3), (12, 32, 0.1), (9, 16, 0.25)]
+    ns = [s[0] for s in specs]
+    truncs = [pkg.Trunc.both(s[1], 1e-12) for s in specs]
+    host = pkg.Batch(ns, truncs, "mixed")
+    dev = pkg.Batch(ns, truncs, "mixed")
+    ptr = dev.device_inputs(max_gates=sum(n // 2 for n in ns), max_meas=sum(ns))
+    view = lambda name, n, ts: torch.as_tensor(_DevView(ptr[name], n, ts), device="cuda")
+    for t in range(8):
+        nt = 4 if t % 3 else 3  # lists of 3 and 4 trajectories
+        trajs = list(range(nt))
+        layers = [pkg.gen_layer(5, i, t, specs[i][0], specs[i][2]) for i in trajs]
+        r_host, e_host = host.step(trajs, layers)
+        pk = pkg.Batch.pack(trajs, layers)
+        nm = int(pk["meas_off"][-1])
+        for name, ts, arr in (("trajs", "<i4", pk["trajs"].astype(np.int32)),
+                              ("gate_off", "<i4", pk["gate_off"].astype(np.int32)),
+                              ("gate_ks", "<i4", pk["gate_ks"].astype(np.int32)),
+                              ("gates", "<f8", pk["gates"]),
+                              ("meas_off", "<i4", pk["meas_off"].astype(np.int32)),
+                              ("meas_ks", "<i4", pk["meas_ks"].astype(np.int32)),
+                              ("us", "<f8", pk["us"])):
+            if arr.size:
+                view(name, arr.size, ts).copy_(torch.from_numpy(np.ascontiguousarray(arr)))
+        torch.cuda.synchronize()
+        dev.step_device(nt)
+        dev.synchronize()
+        ent = view("entropy", nt, "<f8").cpu().numpy()
+        oc = view("outcomes", max(nm, 1), "<i4").cpu().numpy()[:nm]
+        pr = view("probs", max(nm, 1), "<f8").cpu().numpy()[:nm]
+        assert list(ent) == list(e_host)
+        flat = [rec for recs in r_host for rec in recs]
+        assert [int(x[1]) for x in flat] == list(oc)
+        assert [x[2] for x in flat] == list(pr)
+    assert host.device_status() == 0 and dev.device_status() == 0
