@@ -58,8 +58,10 @@ def parse():
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--schedule", type=int, default=1, choices=[0, 1])
-    ap.add_argument("--workload", default="batch", choices=["batch", "mixed", "large"],
-                    help="batch: the headline line; mixed: the batching workload; large: n=128, chi_max=1024")
+    ap.add_argument("--workload", default="batch", choices=["batch", "mixed", "large", "precision"],
+                    help="batch: the headline line; mixed: the batching workload; large: n=128, chi_max=1024; "
+                         "precision: mixed vs float64 errors per p (uses --n, --chi, --depth)")
+    ap.add_argument("--depth", type=int, default=64)
     ap.add_argument("--large-seconds", type=float, default=300.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
@@ -539,6 +541,67 @@ def run_large(a):
             "unit": "s per layer"}
 
 
+def run_precision(a):
+    """Errors of the mixed path against the float64 GPU path (itself held to
+    the FP64 oracle by the parity tests) on identical inputs: per p of the
+    precision workload's set, the largest half-chain entropy difference over
+    the layers, the largest probability difference, and the largest relative
+    Schmidt-value difference (values above 1e-4) at the last layer; compared
+    up to the first layer whose outcome records differ (|p - u| ties)."""
+    import numpy as np
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    n, chi, depth, reps = a.n, a.chi, a.depth, 2
+    specs = [(p, r) for p in P_LIST for r in range(reps)]
+    trajs = [pkg.gen_trajectory(a.seed, 1000 * r + int(p * 100), n, depth, p) for p, r in specs]
+    out = {}
+    runs = {}
+    t0 = time.perf_counter()
+    for prec in ("f64", "mixed"):
+        b = pkg.Batch([n] * len(trajs), [pkg.Trunc.both(chi, a.cutoff)] * len(trajs), prec)
+        ents, recs = [[] for _ in trajs], [[] for _ in trajs]
+        for t in range(depth):
+            r, e = b.step(list(range(len(trajs))), [tl[t] for tl in trajs])
+            for i in range(len(trajs)):
+                ents[i].append(float(e[i]))
+                recs[i].append(r[i])
+        sv = [[b.svals(i, bd) for bd in range(n - 1)] for i in range(len(trajs))]
+        runs[prec] = (ents, recs, sv, b.device_status())
+    for i, (p, r) in enumerate(specs):
+        e64, r64, s64 = runs["f64"][0][i], runs["f64"][1][i], runs["f64"][2][i]
+        e32, r32, s32 = runs["mixed"][0][i], runs["mixed"][1][i], runs["mixed"][2][i]
+        last = depth
+        for t in range(depth):
+            if [x[:2] for x in r64[t]] != [x[:2] for x in r32[t]]:
+                last = t
+                break
+        e_ent = max([abs(e64[t] - e32[t]) for t in range(last)] or [0.0])
+        e_p = max([abs(x[2] - y[2]) for t in range(last) for x, y in zip(r64[t], r32[t])] or [0.0])
+        e_s = None
+        if last == depth:
+            e_s = 0.0
+            for x, y in zip(s64, s32):
+                x, y = np.asarray(x), np.asarray(y)
+                k = min(len(x), len(y))
+                sel = x[:k] > 1e-4
+                if sel.any():
+                    e_s = max(e_s, float(np.max(np.abs(x[:k][sel] - y[:k][sel]) / x[:k][sel])))
+        key = f"p={p}"
+        prev = out.get(key)
+        cur = dict(entropy_abs=e_ent, prob_abs=e_p, schmidt_rel=e_s, layers_compared=last)
+        if prev is None:
+            out[key] = cur
+        else:
+            out[key] = dict(entropy_abs=max(prev["entropy_abs"], e_ent), prob_abs=max(prev["prob_abs"], e_p),
+                            schmidt_rel=None if e_s is None or prev["schmidt_rel"] is None
+                            else max(prev["schmidt_rel"], e_s),
+                            layers_compared=min(prev["layers_compared"], last))
+    return {"workload": f"precision: N={n} chi_max={chi} cutoff={a.cutoff:g} depth {depth}, p in {list(P_LIST)}, "
+                        f"{reps} trajectories per p; mixed vs float64 GPU path on identical inputs",
+            "errors": out, "device_status": {k: v[3] for k, v in runs.items()},
+            "wall_s": time.perf_counter() - t0}
+
+
 def main():
     a = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -577,12 +640,12 @@ def main():
         print(json.dumps(out), flush=True)
         return
 
-    if a.workload in ("mixed", "large"):
+    if a.workload in ("mixed", "large", "precision"):
         if rank != 0:
             return
         import torch
         torch.cuda.set_device(0)
-        out = run_mixed(a) if a.workload == "mixed" else run_large(a)
+        out = {"mixed": run_mixed, "large": run_large, "precision": run_precision}[a.workload](a)
         out.update({"metric": METRIC if a.workload == "mixed" else "per-layer time and entropy",
                     "n_gpus": 1, "data": "synthetic (seeded Haar gates and measurement uniforms)"})
         print(json.dumps(out), flush=True)

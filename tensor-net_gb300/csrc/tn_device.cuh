@@ -20,6 +20,7 @@
 #include <stdint.h>
 
 #include "tn_internal.h"
+#include "tn_tc.cuh"
 
 namespace tn {
 
@@ -190,6 +191,11 @@ struct Smem {
   cpx<T> *Ab, *G, *J, *Ts;  // G and J: W x W, row pitch W + 1
   double *red;
   int *ired;
+  // tensor-core state of the CTA (float executor): accumulator columns in
+  // tensor memory, the MMA-completion mbarrier and its phase
+  uint64_t *bar = nullptr;
+  uint32_t tmem = 0, phase = 0;
+  bool tc = false;
   __device__ Smem(unsigned char *base, int P) {
     using L = SmemLayout<T, W>;
     auto al = [](unsigned char *q) {
@@ -381,6 +387,160 @@ __device__ void build_theta(const cpx<T> *__restrict__ gk, const cpx<T> *__restr
     }
   }
   __syncthreads();
+}
+
+// Waits (every thread) for the MMAs committed to sm.bar; false when they did
+// not complete within 10 s (the caller flags the trajectory).
+template <typename T, int W>
+__device__ bool wait_mma(Smem<T, W> &sm) {
+  const uint64_t t0 = tc::global_ns();
+  bool ok = true;
+  while (!tc::mbar_try_wait(sm.bar, sm.phase)) {
+    if (tc::global_ns() - t0 > 10ull * 1000 * 1000 * 1000) {
+      ok = false;
+      break;
+    }
+  }
+  sm.phase ^= 1u;
+  return ok;
+}
+
+// theta on the tensor cores (float executor): the complex GEMM
+// X (2cL x cM, Gamma_k rows) * Y (cM x 2cR, Lambda_k Gamma_{k+1}) as one real
+// GEMM of the real view of X (interleaved re/im along K) with the 2x2 real
+// embedding [[Yr, Yi], [-Yi, Yr]] of Y, in 128 x 256 tiles of kind::tf32
+// tcgen05.mma with the accumulator in tensor memory.  Each operand is split
+// into a TF32 part and its remainder (3 products: hi*hi + hi*lo + lo*hi,
+// accumulated in FP32), which keeps the products to about 2^-21 relative.
+// Output columns of a tile are ordered (w, s2, re/im), so one thread holds
+// theta[(v, s1), (s2, w)] for both s2 of its row and its partner lane holds
+// the other s1: the Lambda scaling and the 4x4 gate on (s1 s2) are applied in
+// registers before the stores, as in build_theta.  Shared memory: the tiles
+// live in the resident Jacobi block's area, idle while theta is built.
+template <int NT, int W>
+__device__ bool build_theta_tc(const cpx<float> *gk, const cpx<float> *gk1, const float *lamL, const float *lamM,
+                               const float *lamR, int cL, int cM, int cR, const double *gate, cpx<float> *A,
+                               cpx<float> *T0, bool colmode, Smem<float, W> &sm) {
+  constexpr int MT = 128, NTL = 256, KC = 32, WT = NTL / 4;
+  constexpr uint32_t IDESC = tc::idesc_tf32(MT, NTL);
+  constexpr uint32_t LBO = 128, SBO = KC * 32;
+  static_assert(SmemLayout<float, W>::ab_bytes >= size_t(2 * (MT + NTL) * KC) * sizeof(float), "tiles fit");
+  float *Ahi = reinterpret_cast<float *>(sm.Ab), *Alo = Ahi + MT * KC, *Bhi = Alo + MT * KC, *Blo = Bhi + NTL * KC;
+  const int m = 2 * cL, nc = 2 * cR, K2 = 2 * cM;
+  const int ell = colmode ? m : nc;
+  const float *gkf = reinterpret_cast<const float *>(gk);
+  cpx<float> U[16];
+  if (gate) {
+#pragma unroll
+    for (int q = 0; q < 16; ++q) U[q] = mkc<float>(float(gate[2 * q]), float(gate[2 * q + 1]));
+  }
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  bool ok = true;
+  for (int i0 = 0; i0 < m; i0 += MT) {
+    for (int w0 = 0; w0 < cR; w0 += WT) {
+      int chunk = 0;
+      for (int k0 = 0; k0 < K2; k0 += KC, ++chunk) {
+        if (chunk > 0) ok = wait_mma<float, W>(sm) && ok;  // the staging tiles are free again
+        for (int idx = tid; idx < MT * KC; idx += NT) {
+          // idx * 4 bytes == tc::kmajor_offset(r, k, KC)
+          const int core = idx >> 5, within = idx & 31;
+          const int r = (core / (KC / 4)) * 8 + (within >> 2), k = (core % (KC / 4)) * 4 + (within & 3);
+          const int i = i0 + r, kk = k0 + k;
+          const float x = (i < m && kk < K2) ? gkf[size_t(i) * K2 + kk] : 0.f;
+          float hi, lo;
+          tc::split_tf32(x, hi, lo);
+          Ahi[idx] = hi;
+          Alo[idx] = lo;
+        }
+        for (int idx = tid; idx < NTL * KC; idx += NT) {
+          const int core = idx >> 5, within = idx & 31;
+          const int nl = (core / (KC / 4)) * 8 + (within >> 2), k = (core % (KC / 4)) * 4 + (within & 3);
+          const int kk = k0 + k, u = kk >> 1, a = kk & 1;
+          const int b = nl & 1, s2 = (nl >> 1) & 1, w = w0 + (nl >> 2);
+          float x = 0.f;
+          if (u < cM && w < cR) {
+            const cpx<float> y = gk1[size_t(u) * nc + s2 * cR + w];
+            const float l = lamM[u];
+            x = (a == b) ? y.x * l : (a == 0 ? y.y * l : -y.y * l);  // [[Yr, Yi], [-Yi, Yr]]
+          }
+          float hi, lo;
+          tc::split_tf32(x, hi, lo);
+          Bhi[idx] = hi;
+          Blo[idx] = lo;
+        }
+        tc::fence_smem_to_async();
+        __syncthreads();
+        if (tid == 0) {
+          tc::fence_after_sync();
+#pragma unroll
+          for (int st = 0; st < KC / 8; ++st) {
+            const uint32_t off = uint32_t(st) * 2 * LBO;  // 8 K values = two core matrices
+            const uint64_t ah = tc::smem_desc(reinterpret_cast<char *>(Ahi) + off, LBO, SBO);
+            const uint64_t al = tc::smem_desc(reinterpret_cast<char *>(Alo) + off, LBO, SBO);
+            const uint64_t bh = tc::smem_desc(reinterpret_cast<char *>(Bhi) + off, LBO, SBO);
+            const uint64_t bl = tc::smem_desc(reinterpret_cast<char *>(Blo) + off, LBO, SBO);
+            tc::mma_tf32(sm.tmem, ah, bh, IDESC, (chunk > 0 || st > 0) ? 1u : 0u);
+            tc::mma_tf32(sm.tmem, ah, bl, IDESC, 1u);
+            tc::mma_tf32(sm.tmem, al, bh, IDESC, 1u);
+          }
+          tc::mma_commit(sm.bar);
+        }
+      }
+      ok = wait_mma<float, W>(sm) && ok;
+      tc::fence_after_sync();
+      // epilogue: warp w reads lanes 32 (w % 4) .. +31 (rows) and columns 64 (w / 4) .. +63
+      const int sp = warp & 3, cq = warp >> 2;
+      const int i = i0 + 32 * sp + lane;
+      const int v = i >> 1, s1 = i & 1;
+      const float sl = i < m ? lamL[v] : 0.f;
+#pragma unroll 1
+      for (int c16 = 0; c16 < 4; ++c16) {
+        float d[16];
+        tc::tmem_ld16(sm.tmem + (uint32_t(32 * sp) << 16) + uint32_t(64 * cq + 16 * c16), d);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int w = w0 + 16 * cq + 4 * c16 + q;
+          const float sc = sl * (w < cR ? lamR[w] : 0.f);
+          cpx<float> t[2] = {mkc<float>(d[4 * q] * sc, d[4 * q + 1] * sc),
+                             mkc<float>(d[4 * q + 2] * sc, d[4 * q + 3] * sc)};
+          cpx<float> pt[2];
+#pragma unroll
+          for (int s = 0; s < 2; ++s) {
+            pt[s].x = __shfl_xor_sync(0xffffffffu, t[s].x, 1);
+            pt[s].y = __shfl_xor_sync(0xffffffffu, t[s].y, 1);
+          }
+          cpx<float> out[2] = {t[0], t[1]};
+          if (gate) {
+            // th[(s1', s2')]: own row s1' = s1, partner row s1' = 1 - s1
+            cpx<float> th[4];
+            th[2 * s1] = t[0];
+            th[2 * s1 + 1] = t[1];
+            th[2 * (1 - s1)] = pt[0];
+            th[2 * (1 - s1) + 1] = pt[1];
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+              cpx<float> acc = czero<float>();
+#pragma unroll
+              for (int bb = 0; bb < 4; ++bb) acc = cfma(U[(2 * s1 + s) * 4 + bb], th[bb], acc);
+              out[s] = acc;
+            }
+          }
+          if (i < m && w < cR) {
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+              const int j = s * cR + w;
+              const size_t o2 = colmode ? size_t(j) * ell + i : size_t(i) * ell + j;
+              A[o2] = out[s];
+              T0[o2] = out[s];
+            }
+          }
+        }
+      }
+      tc::fence_before_sync();
+      __syncthreads();
+    }
+  }
+  return ok;
 }
 
 // =======================================================================
@@ -1199,8 +1359,20 @@ __device__ void bond_op(const TrajDev &tr, int k, const double *gate, Work<T> &w
   // chiM go through the LQ-reduced matrix M (m x chiM); gates and small
   // bonds take the direct path on theta.
   bool lq = false;
+  // theta on the tensor cores when the CTA has them and the tiles are not
+  // mostly padding; otherwise the SIMT contraction
+  auto theta = [&](const double *g, cpx<T> *dst, cpx<T> *copy, bool cm) {
+    if constexpr (sizeof(T) == 4) {
+      if (sm.tc && m >= 64 && cR >= 16 && cM >= 8) {
+        if (!build_theta_tc<NT, W>(gk, gk1, lLt, lMt, lRt, cL, cM, cR, g, dst, copy, cm, sm) && threadIdx.x == 0)
+          atomicOr(tr.status, ST_BAD_INSTR);
+        return;
+      }
+    }
+    build_theta<T, NT, W>(gk, gk1, lLt, lMt, lRt, cL, cM, cR, g, dst, copy, cm, sm);
+  };
   if (!gate && cM < nc && cM <= m) {
-    build_theta<T, NT, W>(gk, gk1, lLt, lMt, lRt, cL, cM, cR, nullptr, wk.T0, wk.T0, true, sm);
+    theta(nullptr, wk.T0, wk.T0, true);
     lq = refactor_lq<T, NT, W>(gk, gk1, lLt, lMt, lRt, cL, cM, cR, tr.cap, wk, sm);
   }
   bool colmode;
@@ -1213,7 +1385,7 @@ __device__ void bond_op(const TrajDev &tr, int k, const double *gate, Work<T> &w
     colmode = m > nc;  // square: vectors = rows (coalesced theta stores)
     ell = colmode ? m : nc;
     c = colmode ? nc : m;
-    build_theta<T, NT, W>(gk, gk1, lLt, lMt, lRt, cL, cM, cR, gate, wk.A, wk.T0, colmode, sm);
+    theta(gate, wk.A, wk.T0, colmode);
   }
   long long c1 = clock64();
   long long cyc[4] = {0, 0, 0, 0};

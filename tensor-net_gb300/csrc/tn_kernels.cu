@@ -10,14 +10,11 @@
 //               mps.rs:370-391).
 #include "tn_device.cuh"
 #include "tn_internal.h"
+#include "tn_tc.cuh"
 
 namespace tn {
 
-__device__ __forceinline__ unsigned long long global_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-  return t;
-}
+__device__ __forceinline__ unsigned long long global_ns() { return tc::global_ns(); }
 
 __device__ __forceinline__ int load_acquire(const int *p) {
   int v;
@@ -49,9 +46,31 @@ __global__ void __launch_bounds__(NT, 1) k_run(LaunchArgs la, int sortP, int ws_
   extern __shared__ __align__(256) unsigned char smem[];
   __shared__ Item s_item;
   __shared__ int s_kind;  // 0 done, 1 gate / static item, 2 pushed sweep item, 3 skip
+  __shared__ uint64_t s_bar;
+  __shared__ uint32_t s_tmem;
   Smem<T, W> sm(smem, sortP);
   Work<T> wk = make_work<T>(reinterpret_cast<unsigned char *>(la.ws) + size_t(blockIdx.x) * la.ws_stride, ws_cap);
   const bool dd = la.rem != nullptr;
+  constexpr uint32_t kTmemCols = 256;  // one 128 x 256 FP32 accumulator tile
+  if constexpr (sizeof(T) == 4) {
+    // the float executor owns kTmemCols tensor-memory columns for its whole
+    // life (one CTA per SM); released below on the kernel's only exit path
+    if ((threadIdx.x >> 5) == 0) {
+      tc::tmem_alloc(&s_tmem, kTmemCols);
+      tc::tmem_relinquish();
+    }
+    if (threadIdx.x == 0) {
+      tc::mbar_init(&s_bar, 1);
+      tc::mbar_fence_init();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    sm.tmem = s_tmem;
+    sm.bar = &s_bar;
+    sm.phase = 0;
+    sm.tc = true;
+  }
   for (;;) {
     if (threadIdx.x == 0) {
       const int it = atomicAdd(la.counter, 1);
@@ -87,7 +106,18 @@ __global__ void __launch_bounds__(NT, 1) k_run(LaunchArgs la, int sortP, int ws_
     if (dd && kind == 1) {
       __threadfence();  // this thread's writes of the gate's result, visible device-wide
       __syncthreads();
-      if (threadIdx.x == 0 && atomicSub(la.rem + item.aux, 1) == 1) push_sweep(la.dyn, la.dyn_tail, la.sweeps, item.aux);
+      if (threadIdx.x == 0 && atomicSub(la.rem + item.aux, 1) == 1) {
+        __threadfence();
+        push_sweep(la.dyn, la.dyn_tail, la.sweeps, item.aux);
+      }
+    }
+  }
+  if constexpr (sizeof(T) == 4) {
+    tc::fence_before_sync();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) {
+      tc::fence_after_sync();
+      tc::tmem_dealloc(sm.tmem, kTmemCols);
     }
   }
 }
