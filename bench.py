@@ -62,6 +62,8 @@ def parse():
                     help="batch: the headline line; mixed: the batching workload; large: n=128, chi_max=1024; "
                          "precision: mixed vs float64 errors per p (uses --n, --chi, --depth)")
     ap.add_argument("--depth", type=int, default=64)
+    ap.add_argument("--theta", default="tc", choices=["tc", "simt"],
+                    help="mixed precision theta contraction: tensor cores (tcgen05) or SIMT FP32")
     ap.add_argument("--large-seconds", type=float, default=300.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
@@ -271,6 +273,7 @@ def run_gpu(a, rank, world, local_rank):
     trunc = pkg.Trunc.both(chi, a.cutoff)
     batch = pkg.Batch([n] * B, [trunc] * B, a.prec)
     batch.set_schedule(a.schedule)
+    batch.set_theta_path(a.theta == "simt")
     traj0 = rank * B
     total_layers = a.prefill + a.warmup + 2 * a.steps
 
@@ -559,6 +562,7 @@ def run_precision(a):
     t0 = time.perf_counter()
     for prec in ("f64", "mixed"):
         b = pkg.Batch([n] * len(trajs), [pkg.Trunc.both(chi, a.cutoff)] * len(trajs), prec)
+        b.set_theta_path(a.theta == "simt")
         ents, recs = [[] for _ in trajs], [[] for _ in trajs]
         for t in range(depth):
             r, e = b.step(list(range(len(trajs))), [tl[t] for tl in trajs])
@@ -596,8 +600,15 @@ def run_precision(a):
                             schmidt_rel=None if e_s is None or prev["schmidt_rel"] is None
                             else max(prev["schmidt_rel"], e_s),
                             layers_compared=min(prev["layers_compared"], last))
-    return {"workload": f"precision: N={n} chi_max={chi} cutoff={a.cutoff:g} depth {depth}, p in {list(P_LIST)}, "
+    growth = {}
+    for p in P_LIST:
+        idx = [i for i, (pp, r) in enumerate(specs) if pp == p]
+        growth[f"p={p}"] = [max(abs(runs["f64"][0][i][t] - runs["mixed"][0][i][t]) for i in idx)
+                            for t in range(0, depth, max(1, depth // 16))]
+    return {"entropy_abs_every_few_layers": growth,
+            "workload": f"precision: N={n} chi_max={chi} cutoff={a.cutoff:g} depth {depth}, p in {list(P_LIST)}, "
                         f"{reps} trajectories per p; mixed vs float64 GPU path on identical inputs",
+            "theta_path": a.theta,
             "errors": out, "device_status": {k: v[3] for k, v in runs.items()},
             "wall_s": time.perf_counter() - t0}
 

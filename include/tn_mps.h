@@ -245,6 +245,22 @@ int tn_batch_device_status(tn_batch *b, int32_t *status);
 int tn_batch_stats(tn_batch *b, double *out, int32_t reset);
 /* Device bytes held by slot t (its footprint for admission control). */
 int tn_batch_slot_bytes(tn_batch *b, uint32_t t, uint64_t *bytes);
+/* theta contraction of the mixed-precision executor: 0 (default) tensor
+ * cores (tcgen05, 3xTF32) where the tile shape applies, 1 the SIMT FP32
+ * contraction everywhere.  No counterpart in the reference. */
+int tn_batch_set_theta_path(tn_batch *b, int32_t simt);
+/* Online autotuner: the next 4 * trial_steps host- or pointer-launched steps
+ * (tn_batch_step, tn_batch_step_ptrs) run, trial_steps each, the candidate
+ * configurations {schedule 1, Jacobi scheme 0, tensor-core theta},
+ * {1, 1, tensor-core}, {0, 0, tensor-core}, {1, 0, SIMT theta}; each is
+ * scored by device launch time per algorithmic flop (device counters), and
+ * the best is kept (captured graphs are re-captured with it).  trial_steps
+ * = 0 stops tuning.  Results are the same under every candidate up to the
+ * rounding of the chosen arithmetic.  No counterpart in the reference. */
+int tn_batch_autotune(tn_batch *b, uint32_t trial_steps);
+/* cfg[4]: schedule, Jacobi scheme, SIMT theta (1) / tensor-core theta (0),
+ * tuning in progress; scores[4] (may be NULL): seconds per flop per candidate. */
+int tn_batch_tuning(tn_batch *b, int32_t *cfg, double *scores);
 /* Schedule of a layer step: 1 (default) = one persistent launch in which
  * every gate of the layer is a work item and a trajectory's measurement
  * layer, refactor sweep and entropy read become a work item as soon as its

@@ -86,6 +86,9 @@ SIGNATURES = {
     "tn_batch_set_tuning": (C.c_int, [vp, i32, i32]),
     "tn_server_create": (C.c_int, [u64, u32, i32, u32, u32, P(vp)]),
     "tn_batch_set_schedule": (C.c_int, [vp, i32]),
+    "tn_batch_autotune": (C.c_int, [vp, u32]),
+    "tn_batch_set_theta_path": (C.c_int, [vp, i32]),
+    "tn_batch_tuning": (C.c_int, [vp, P(i32), P(dbl)]),
     "tn_server_create_classes": (C.c_int, [u64, u32, i32, u32, u32, u32, u32, P(vp)]),
     "tn_server_class_stats": (C.c_int, [vp, u32, P(dbl)]),
     "tn_server_set_policy": (C.c_int, [vp, i32, u32, u32]),

@@ -154,6 +154,20 @@ class Batch:
         """1: one launch per layer (sweeps pushed as their gates finish); 0: two launches."""
         L.check(self._lib.tn_batch_set_schedule(self._h, int(schedule)), "set_schedule")
 
+    def set_theta_path(self, simt: bool = False):
+        """Mixed precision: SIMT FP32 theta contraction (True) or tensor cores (False, default)."""
+        L.check(self._lib.tn_batch_set_theta_path(self._h, int(bool(simt))), "set_theta_path")
+
+    def autotune(self, trial_steps: int = 1):
+        """Tune schedule / Jacobi scheme / theta path over the next 4 * trial_steps steps."""
+        L.check(self._lib.tn_batch_autotune(self._h, int(trial_steps)), "autotune")
+
+    def tuning(self):
+        cfg = (L.i32 * 4)()
+        sc = np.zeros(4)
+        L.check(self._lib.tn_batch_tuning(self._h, cfg, L.dptr(sc)), "tuning")
+        return dict(schedule=cfg[0], scheme=cfg[1], theta_simt=cfg[2], tuning=bool(cfg[3]), scores=list(sc))
+
     def last_launch_ms(self):
         """(gate launch ms, sweep launch ms) of the last non-graph step; with
         the one-launch schedule the first is the whole launch and the second 0."""

@@ -52,6 +52,16 @@ struct tn_batch {
   int sms = 1, bps = 1, grid_max = 1;
   int maxcap = 1, maxn = 1, sortP = 1, pcap = 8;
   int scheme = 0, max_sweeps = 40;  // Jacobi tuning (tn_batch_set_tuning)
+  int theta_simt = 0;               // 1: SIMT theta contraction instead of the tensor-core one
+  // Online autotuner (tn_batch_autotune): the next steps run each candidate
+  // configuration for `trial` steps; the score of a candidate is launch time
+  // per algorithmic flop (both measured on the device); the best one stays.
+  struct Tuner {
+    bool on = false, pending = false;
+    int trial = 1, cand = 0, in_cand = 0;
+    double flops0 = 0;
+    std::vector<double> score;
+  } tune;
   std::vector<uint32_t> n_alloc, cap;
   std::vector<TrajDev> h;
   std::vector<size_t> slot_bytes;
@@ -187,6 +197,60 @@ StepPtrs ptrs_of(const StepLayout &L, char *dbase) {
   return p;
 }
 
+// Candidate configurations of the autotuner: {schedule, Jacobi scheme, SIMT theta}.
+constexpr int kTuneCands = 4;
+constexpr int kTuneTable[kTuneCands][3] = {{1, 0, 0}, {1, 1, 0}, {0, 0, 0}, {1, 0, 1}};
+
+// Algorithmic flops counted so far over every slot (theta + SVD counters).
+int stats_flops(tn_batch *b, double *flops) {
+  std::vector<double> v(size_t(STAT_N) * b->ntraj);
+  CKB(cudaMemcpyAsync(v.data(), b->dstats, sizeof(double) * v.size(), cudaMemcpyDeviceToHost, b->st));
+  CKB(cudaStreamSynchronize(b->st));
+  double f = 0.0;
+  for (uint32_t t = 0; t < b->ntraj; ++t) f += v[size_t(t) * STAT_N + STAT_FLOP_THETA] + v[size_t(t) * STAT_N + STAT_FLOP_SVD];
+  *flops = f;
+  return TN_OK;
+}
+
+void apply_cfg(tn_batch *b, int c) {
+  b->schedule = kTuneTable[c][0];
+  b->scheme = kTuneTable[c][1];
+  b->theta_simt = kTuneTable[c][2];
+}
+
+// Before a host-launched step: score the previous trial step, move on, and
+// apply the configuration of this step.
+int tune_before(tn_batch *b) {
+  tn_batch::Tuner &T = b->tune;
+  if (!T.on) return TN_OK;
+  if (T.pending) {
+    CKB(cudaEventSynchronize(b->ev[2]));
+    float g = 0.f, w = 0.f;
+    CKB(cudaEventElapsedTime(&g, b->ev[0], b->ev[1]));
+    if (!b->ev_one_launch) CKB(cudaEventElapsedTime(&w, b->ev[1], b->ev[2]));
+    double f1 = 0.0;
+    if (int s = stats_flops(b, &f1)) return s;
+    const double df = f1 - T.flops0;
+    T.score[T.cand] += df > 0 ? 1e-3 * (g + w) / df : 0.0;
+    T.pending = false;
+    if (++T.in_cand >= T.trial) {
+      T.in_cand = 0;
+      if (++T.cand >= kTuneCands) {  // done: keep the best
+        int best = 0;
+        for (int c = 1; c < kTuneCands; ++c)
+          if (T.score[c] < T.score[best]) best = c;
+        apply_cfg(b, best);
+        T.on = false;
+        for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
+        b->graphs.clear();
+        return TN_OK;
+      }
+    }
+  }
+  apply_cfg(b, T.cand);
+  return stats_flops(b, &T.flops0);
+}
+
 int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P0, bool timed = true) {
   StepPtrs P = P0;
   if (!P.order) {  // most expensive trajectories first, by their current bond dimensions
@@ -205,6 +269,7 @@ int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P0, bool timed = true)
   la.ws_stride = b->ws_stride;
   la.max_sweeps = b->max_sweeps;
   la.jacobi_scheme = b->scheme;
+  la.theta_simt = b->theta_simt;
   la.qerr = b->dcounter + 9;
   const int gmax = b->grid_limit > 0 ? std::min(b->grid_limit, b->grid_max) : b->grid_max;
   if (b->schedule == 1) {
@@ -234,6 +299,7 @@ int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P0, bool timed = true)
       CKB(cudaEventRecord(b->ev[2], b->st));
       b->ev_recorded = true;
       b->ev_one_launch = true;
+      b->tune.pending = b->tune.on;
     }
     return TN_OK;
   }
@@ -261,6 +327,7 @@ int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P0, bool timed = true)
     CKB(cudaEventRecord(b->ev[2], b->st));
     b->ev_recorded = true;
     b->ev_one_launch = false;
+    b->tune.pending = b->tune.on;
   }
   return TN_OK;
 }
@@ -468,6 +535,7 @@ int tn_batch_step(tn_batch *b, const uint32_t *trajs, uint32_t nt, const uint32_
   for (uint32_t j = 0; j < nm; ++j) mk[j] = int(meas_ks[j]);
   if (ng) std::memcpy(hb + L.gates, gates, sizeof(double) * 32 * ng);
   if (nm) std::memcpy(hb + L.us, us, sizeof(double) * nm);
+  if (int s = tune_before(b)) return s;
   CKB(cudaMemcpyAsync(b->dstep, b->hstep, L.in_bytes, cudaMemcpyHostToDevice, b->st));
   StepPtrs P = ptrs_of(L, reinterpret_cast<char *>(b->dstep));
   P.order = nullptr;  // ranked on the device from the current bond dimensions
@@ -557,6 +625,7 @@ int tn_batch_step_ptrs(tn_batch *b, uint32_t nt, const void *d_trajs, const void
   P.outc = static_cast<int *>(d_outcomes);
   P.probs = static_cast<double *>(d_probs);
   P.ents = static_cast<double *>(d_entropy);
+  if (int s = tune_before(b)) return s;
   return launch_step(b, nt, P);
 }
 
@@ -623,6 +692,37 @@ int tn_batch_device_status(tn_batch *b, int32_t *status) {
 int tn_batch_slot_bytes(tn_batch *b, uint32_t t, uint64_t *bytes) {
   if (!b || t >= b->ntraj || !bytes) return TN_ERR_INVALID_ARG;
   *bytes = b->slot_bytes[t];
+  return TN_OK;
+}
+
+int tn_batch_autotune(tn_batch *b, uint32_t trial_steps) {
+  if (!b) return TN_ERR_INVALID_ARG;
+  tn_batch::Tuner &T = b->tune;
+  T.on = trial_steps > 0;
+  T.pending = false;
+  T.trial = int(std::max<uint32_t>(trial_steps, 1));
+  T.cand = 0;
+  T.in_cand = 0;
+  T.score.assign(kTuneCands, 0.0);
+  return TN_OK;
+}
+
+int tn_batch_tuning(tn_batch *b, int32_t *cfg, double *scores) {
+  if (!b || !cfg) return TN_ERR_INVALID_ARG;
+  cfg[0] = b->schedule;
+  cfg[1] = b->scheme;
+  cfg[2] = b->theta_simt;
+  cfg[3] = b->tune.on ? 1 : 0;
+  if (scores)
+    for (int c = 0; c < kTuneCands; ++c) scores[c] = c < int(b->tune.score.size()) ? b->tune.score[c] : 0.0;
+  return TN_OK;
+}
+
+int tn_batch_set_theta_path(tn_batch *b, int32_t simt) {
+  if (!b || simt < 0 || simt > 1) return TN_ERR_INVALID_ARG;
+  for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
+  b->graphs.clear();
+  b->theta_simt = simt;
   return TN_OK;
 }
 

@@ -92,6 +92,7 @@ struct LaunchArgs {
   size_t ws_stride;      // bytes per CTA
   int max_sweeps;
   int jacobi_scheme;      // 0: block pairs, all pairs per step; 1: within-block then cross-block steps
+  int theta_simt;         // 1: SIMT theta contraction even where the tensor-core one applies
   // Dependency-driven schedule (rem != nullptr): items[0, *nitems_dev) are
   // gate items with programs in gprog; when the last gate item of listed
   // trajectory i finishes, its sweep item sweeps[i] is pushed to dyn, and the

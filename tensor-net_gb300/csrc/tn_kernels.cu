@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(NT, 1) k_run(LaunchArgs la, int sortP, int ws_
     sm.tmem = s_tmem;
     sm.bar = &s_bar;
     sm.phase = 0;
-    sm.tc = true;
+    sm.tc = la.theta_simt == 0;
   }
   for (;;) {
     if (threadIdx.x == 0) {

@@ -299,3 +299,35 @@ def test_graph_captured_step_matches_host_step(pkg):
         assert [int(x[1]) for x in flat] == list(oc)
         assert [x[2] for x in flat] == list(pr)
     assert host.device_status() == 0 and dev.device_status() == 0
+
+
+def test_autotuner_tries_every_candidate_and_keeps_the_best(pkg):
+    """tn_batch_autotune runs each candidate configuration (schedule, Jacobi
+    scheme, tensor-core / SIMT theta) for its trial steps, scores it by
+    device time per algorithmic flop and keeps the best; results stay within
+    the mixed-precision tolerance of an untuned batch on the same inputs."""
+    specs = [(12, 32, 0.1), (14, 64, 0.05), (10, 16, 0.2), (16, 64, 0.15)]
+    ns = [s[0] for s in specs]
+    truncs = [pkg.Trunc.both(s[1], 1e-10) for s in specs]
+    tuned = pkg.Batch(ns, truncs, "mixed")
+    plain = pkg.Batch(ns, truncs, "mixed")
+    order = list(range(len(specs)))
+    for t in range(6):  # grow entanglement first so that every candidate does real work
+        layers = [pkg.gen_layer(9, i, t, s[0], s[2]) for i, s in enumerate(specs)]
+        tuned.step(order, layers)
+        plain.step(order, layers)
+    tuned.autotune(1)
+    assert tuned.tuning()["tuning"]
+    for t in range(6, 12):
+        layers = [pkg.gen_layer(9, i, t, s[0], s[2]) for i, s in enumerate(specs)]
+        r1, e1 = tuned.step(order, layers)
+        r0, e0 = plain.step(order, layers)
+        assert [[x[:2] for x in a] for a in r1] == [[x[:2] for x in a] for a in r0]
+        np.testing.assert_allclose(e1, e0, atol=1e-4)
+    st = tuned.tuning()
+    assert not st["tuning"]
+    assert all(s > 0 for s in st["scores"])
+    best = int(np.argmin(st["scores"]))
+    cand = [(1, 0, 0), (1, 1, 0), (0, 0, 0), (1, 0, 1)][best]
+    assert (st["schedule"], st["scheme"], st["theta_simt"]) == cand
+    assert tuned.device_status() == 0
