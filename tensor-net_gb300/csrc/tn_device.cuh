@@ -196,6 +196,7 @@ struct Smem {
   uint64_t *bar = nullptr;
   uint32_t tmem = 0, phase = 0;
   bool tc = false;
+  bool tc_fail = false;  // an MMA wait ran past its limit during the current bond op
   __device__ Smem(unsigned char *base, int P) {
     using L = SmemLayout<T, W>;
     auto al = [](unsigned char *q) {
@@ -402,6 +403,7 @@ __device__ bool wait_mma(Smem<T, W> &sm) {
     }
   }
   sm.phase ^= 1u;
+  if (!ok) sm.tc_fail = true;
   return ok;
 }
 
@@ -1116,6 +1118,106 @@ __device__ void gemm_nt(int M, int N, int K, FP P, FQ Q, FE E, Smem<T, W> &sm) {
   __syncthreads();
 }
 
+// C[x][y] = sum_k P(x, k) Q(y, k) (complex) on the tensor cores: the real view
+// of P (interleaved re/im along K) times the 2x2 real embedding of Q, in
+// 128 x 256 tcgen05 kind::tf32 tiles with 3xTF32 splitting, as in
+// build_theta_tc; output columns of a tile ordered (y, re/im); E(x, y, v)
+// stores.  Staging tiles in the resident Jacobi block's shared memory, which
+// is idle outside the Jacobi.
+template <int NT, int W, class FP, class FQ, class FE>
+__device__ bool gemm_nt_tc(int M, int N, int K, FP P, FQ Q, FE E, Smem<float, W> &sm) {
+  constexpr int MT = 128, NTL = 256, KC = 32, YT = NTL / 2;
+  constexpr uint32_t IDESC = tc::idesc_tf32(MT, NTL);
+  constexpr uint32_t LBO = 128, SBO = KC * 32;
+  float *Ahi = reinterpret_cast<float *>(sm.Ab), *Alo = Ahi + MT * KC, *Bhi = Alo + MT * KC, *Blo = Bhi + NTL * KC;
+  const int K2 = 2 * K;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  bool ok = true;
+  for (int i0 = 0; i0 < M; i0 += MT) {
+    for (int y0 = 0; y0 < N; y0 += YT) {
+      int chunk = 0;
+      for (int k0 = 0; k0 < K2; k0 += KC, ++chunk) {
+        if (chunk > 0) ok = wait_mma<float, W>(sm) && ok;
+        for (int idx = tid; idx < MT * KC; idx += NT) {
+          const int core = idx >> 5, within = idx & 31;
+          const int r = (core / (KC / 4)) * 8 + (within >> 2), kr = (core % (KC / 4)) * 4 + (within & 3);
+          const int x = i0 + r, kk = k0 + kr;
+          float v = 0.f;
+          if (x < M && kk < K2) {
+            const cpx<float> a = P(x, kk >> 1);
+            v = (kk & 1) ? a.y : a.x;
+          }
+          float hi, lo;
+          tc::split_tf32(v, hi, lo);
+          Ahi[idx] = hi;
+          Alo[idx] = lo;
+        }
+        for (int idx = tid; idx < NTL * KC; idx += NT) {
+          const int core = idx >> 5, within = idx & 31;
+          const int nl = (core / (KC / 4)) * 8 + (within >> 2), kr = (core % (KC / 4)) * 4 + (within & 3);
+          const int kk = k0 + kr, a = kk & 1, b = nl & 1, y = y0 + (nl >> 1);
+          float v = 0.f;
+          if (y < N && kk < K2) {
+            const cpx<float> q = Q(y, kk >> 1);
+            v = (a == b) ? q.x : (a == 0 ? q.y : -q.y);  // [[Qr, Qi], [-Qi, Qr]]
+          }
+          float hi, lo;
+          tc::split_tf32(v, hi, lo);
+          Bhi[idx] = hi;
+          Blo[idx] = lo;
+        }
+        tc::fence_smem_to_async();
+        __syncthreads();
+        if (tid == 0) {
+          tc::fence_after_sync();
+#pragma unroll
+          for (int st = 0; st < KC / 8; ++st) {
+            const uint32_t off = uint32_t(st) * 2 * LBO;
+            const uint64_t ah = tc::smem_desc(reinterpret_cast<char *>(Ahi) + off, LBO, SBO);
+            const uint64_t al = tc::smem_desc(reinterpret_cast<char *>(Alo) + off, LBO, SBO);
+            const uint64_t bh = tc::smem_desc(reinterpret_cast<char *>(Bhi) + off, LBO, SBO);
+            const uint64_t bl = tc::smem_desc(reinterpret_cast<char *>(Blo) + off, LBO, SBO);
+            tc::mma_tf32(sm.tmem, ah, bh, IDESC, (chunk > 0 || st > 0) ? 1u : 0u);
+            tc::mma_tf32(sm.tmem, ah, bl, IDESC, 1u);
+            tc::mma_tf32(sm.tmem, al, bh, IDESC, 1u);
+          }
+          tc::mma_commit(sm.bar);
+        }
+      }
+      ok = wait_mma<float, W>(sm) && ok;
+      tc::fence_after_sync();
+      const int sp = warp & 3, cq = warp >> 2;
+      const int x = i0 + 32 * sp + lane;
+#pragma unroll 1
+      for (int c16 = 0; c16 < 4; ++c16) {
+        float d[16];
+        tc::tmem_ld16(sm.tmem + (uint32_t(32 * sp) << 16) + uint32_t(64 * cq + 16 * c16), d);
+        if (x < M) {
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int y = y0 + 32 * cq + 8 * c16 + q;
+            if (y < N) E(x, y, mkc<float>(d[2 * q], d[2 * q + 1]));
+          }
+        }
+      }
+      tc::fence_before_sync();
+      __syncthreads();
+    }
+  }
+  return ok;
+}
+
+// gemm_nt on the tensor cores when the executor has them (float) and the
+// product is large enough to fill the tiles, else on the SIMT path.
+template <typename T, int NT, int W, class FP, class FQ, class FE>
+__device__ bool gemm_nt_auto(int M, int N, int K, FP P, FQ Q, FE E, Smem<T, W> &sm) {
+  if constexpr (sizeof(T) == 4) {
+    if (sm.tc && M >= 64 && N >= 32 && K >= 16) return gemm_nt_tc<NT, W>(M, N, K, P, Q, E, sm);
+  }
+  gemm_nt<T, NT, W>(M, N, K, P, Q, E, sm);
+  return true;
+}
+
 template <typename T, int NT, int W>
 __device__ void finalize_bond(const TrajDev &tr, int k, cpx<T> *__restrict__ gk, cpx<T> *__restrict__ gk1,
                               const double *__restrict__ lamL, double *__restrict__ lamM,
@@ -1214,7 +1316,7 @@ __device__ void finalize_bond(const TrajDev &tr, int k, cpx<T> *__restrict__ gk,
       gk[idx] = cscale(A[size_t(perm[j]) * ell + i], isig[j] * sclL[i >> 1]);
     }
     // Vh[j][col] = sum_i conj(a_src[i]) theta[i][col] / sigma^2 (recovered)
-    gemm_nt<T, NT, W>(
+    gemm_nt_auto<T, NT, W>(
         rank, nc, m,
         [&](int j, int i) {
           cpx<T> a = A[size_t(perm[j]) * ell + i];
@@ -1229,7 +1331,7 @@ __device__ void finalize_bond(const TrajDev &tr, int k, cpx<T> *__restrict__ gk,
       gk1[idx] = cscale(A[size_t(perm[j]) * ell + col], isig[j] * sclR[col % cR]);
     }
     // U[i][j] = sum_col theta[i][col] conj(w_src[col]) / sigma^2 (recovered)
-    gemm_nt<T, NT, W>(
+    gemm_nt_auto<T, NT, W>(
         m, rank, nc, [&](int i, int col) { return T0[size_t(i) * nc + col]; },
         [&](int j, int col) {
           cpx<T> a = A[size_t(perm[j]) * ell + col];
@@ -1319,7 +1421,7 @@ __device__ bool refactor_lq(const cpx<T> *__restrict__ gk, const cpx<T> *__restr
   const int m = 2 * cL, nc = 2 * cR;
   cpx<T> *S = wk.A + size_t(2) * cap * cap;  // chiM x chiM, after M's m x chiM region
   // S = B B^H
-  gemm_nt<T, NT, W>(
+  gemm_nt_auto<T, NT, W>(
       cM, cM, nc, [&](int x, int col) { return cscale(gk1[size_t(x) * nc + col], lamR[col % cR]); },
       [&](int y, int col) {
         cpx<T> b = cscale(gk1[size_t(y) * nc + col], lamR[col % cR]);
@@ -1330,7 +1432,7 @@ __device__ bool refactor_lq(const cpx<T> *__restrict__ gk, const cpx<T> *__restr
   if (!cholesky_lower<T, NT, W>(S, cM, rel, wk.sig, sm)) return false;
   // M = X diag(Lambda_k) L, stored vector-contiguous: A[j*m + i] = M[i][j]
   cpx<T> *A = wk.A;
-  gemm_nt<T, NT, W>(
+  gemm_nt_auto<T, NT, W>(
       m, cM, cM,
       [&](int i, int u) { return cscale(gk[size_t(i) * cM + u], lamL[i >> 1] * lamM[u]); },
       [&](int j, int u) { return u >= j ? S[size_t(u) * cM + j] : czero<T>(); },
@@ -1364,8 +1466,7 @@ __device__ void bond_op(const TrajDev &tr, int k, const double *gate, Work<T> &w
   auto theta = [&](const double *g, cpx<T> *dst, cpx<T> *copy, bool cm) {
     if constexpr (sizeof(T) == 4) {
       if (sm.tc && m >= 64 && cR >= 16 && cM >= 8) {
-        if (!build_theta_tc<NT, W>(gk, gk1, lLt, lMt, lRt, cL, cM, cR, g, dst, copy, cm, sm) && threadIdx.x == 0)
-          atomicOr(tr.status, ST_BAD_INSTR);
+        build_theta_tc<NT, W>(gk, gk1, lLt, lMt, lRt, cL, cM, cR, g, dst, copy, cm, sm);
         return;
       }
     }
@@ -1413,6 +1514,10 @@ __device__ void bond_op(const TrajDev &tr, int k, const double *gate, Work<T> &w
     }
   }
   finalize_bond<T, NT, W>(tr, k, gk, gk1, lamL, lamM, lamR, cL, cR, colmode, ell, c, wk, sm);
+  if (sm.tc_fail) {  // a tensor-core wait gave up: the op's result is not trustworthy
+    if (threadIdx.x == 0) atomicOr(tr.status, ST_BAD_INSTR);
+    sm.tc_fail = false;
+  }
   if (threadIdx.x == 0 && tr.stats) {
     atomicAdd(tr.stats + STAT_CYC_THETA, double(c1 - c0));
     atomicAdd(tr.stats + STAT_CYC_GRAM, double(cyc[0]));
