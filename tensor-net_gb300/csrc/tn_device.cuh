@@ -756,159 +756,6 @@ __device__ void update_res(int ell, const cpx<T> *__restrict__ Jm, Smem<T, W> &s
   __syncthreads();
 }
 
-// -- resident path on the tensor cores (float executor with tensor memory) --
-// G = Ab^H Ab.  X = real view of the resident block (ell x 64, X[r][2p + a] =
-// part a of Ab[r][p]) is staged per 32-row chunk as the 128-row K-major
-// operand [X_hi^T ; X_lo^T] (rows 0-63 the TF32 parts of the 64 real
-// columns, rows 64-127 the remainders); its two halves are the N=64 B
-// operands, so D = A X_hi + A X_lo holds hi*hi + hi*lo (rows 0-63) and
-// lo*hi + lo*lo (rows 64-127) of X^T X.  Region 0 holds the staging tile,
-// then the lower half of D for the final sum.
-template <int NT, int W>
-__device__ void gram_tc(int ell, Smem<float, W> &sm) {
-  static_assert(W == 32 && NT == 512, "tensor-core Gram layout");
-  constexpr int TP = W + 1, GP = W + 1, MT = 128, NN = 64, KC = 32, SP = NN + 1;
-  constexpr uint32_t IDESC = tc::idesc_tf32(MT, NN), LBO = 128, SBO = KC * 32;
-  static_assert(SmemLayout<float, W>::gemm_bytes >= size_t(NN) * SP * sizeof(float), "D half fits region 0");
-  static_assert(SmemLayout<float, W>::theta_bytes >= size_t(MT) * KC * sizeof(float), "tile fits region 0");
-  float *T = reinterpret_cast<float *>(sm.r0);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  int chunk = 0;
-  for (int k0 = 0; k0 < ell; k0 += KC, ++chunk) {
-    if (chunk > 0) wait_mma<float, W>(sm);
-    for (int idx = tid; idx < MT * KC; idx += NT) {
-      const int core = idx >> 5, within = idx & 31;
-      const int m = (core / (KC / 4)) * 8 + (within >> 2), k = (core % (KC / 4)) * 4 + (within & 3);
-      const int r = k0 + k, col = m & 63;
-      float v = 0.f;
-      if (r < ell) {
-        const cpx<float> x = sm.Ab[r * TP + (col >> 1)];
-        v = (col & 1) ? x.y : x.x;
-      }
-      float hi, lo;
-      tc::split_tf32(v, hi, lo);
-      T[idx] = m < NN ? hi : lo;
-    }
-    tc::fence_smem_to_async();
-    __syncthreads();
-    if (tid == 0) {
-      tc::fence_after_sync();
-#pragma unroll
-      for (int st = 0; st < KC / 8; ++st) {
-        const uint32_t off = uint32_t(st) * 2 * LBO;
-        const uint64_t a = tc::smem_desc(reinterpret_cast<char *>(T) + off, LBO, SBO);
-        const uint64_t bl = tc::smem_desc(reinterpret_cast<char *>(T) + (NN / 8) * SBO + off, LBO, SBO);
-        tc::mma_tf32(sm.tmem, a, a, IDESC, (chunk > 0 || st > 0) ? 1u : 0u);  // B = rows 0-63 (X_hi)
-        tc::mma_tf32(sm.tmem, a, bl, IDESC, 1u);                              // B = rows 64-127 (X_lo)
-      }
-      tc::mma_commit(sm.bar);
-    }
-  }
-  wait_mma<float, W>(sm);
-  tc::fence_after_sync();
-  const int sp = warp & 3, cb = warp >> 2, row = 32 * sp + lane;
-  float d[16];
-  tc::tmem_ld16(sm.tmem + (uint32_t(32 * sp) << 16) + uint32_t(16 * cb), d);
-  if (sp >= 2) {
-#pragma unroll
-    for (int c = 0; c < 16; ++c) T[(row - NN) * SP + 16 * cb + c] = d[c];
-  }
-  __syncthreads();
-  if (sp < 2) {
-#pragma unroll
-    for (int c = 0; c < 16; ++c) d[c] += T[row * SP + 16 * cb + c];
-    // row = 2p + a; the partner lane holds the other part of the same p
-    float e[16];
-#pragma unroll
-    for (int c = 0; c < 16; ++c) e[c] = __shfl_xor_sync(0xffffffffu, d[c], 1);
-    if ((row & 1) == 0) {
-      const int pp = row >> 1;
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        // XX[2p][2q] + XX[2p+1][2q+1],  XX[2p][2q+1] - XX[2p+1][2q]
-        sm.G[pp * GP + 8 * cb + j] = mkc<float>(d[2 * j] + e[2 * j + 1], d[2 * j + 1] - e[2 * j]);
-      }
-    }
-  }
-  tc::fence_before_sync();
-  __syncthreads();
-}
-
-// Ab <- Ab J on the tensor cores: per 128-row tile of X, D = X_tile Jr with Jr
-// the 64 x 64 real embedding of J ([[Jr, Ji], [-Ji, Jr]] per entry), in K
-// chunks of 16 real columns (A = X rows, B = Jr columns, both K-major, split;
-// A in region 0, B in Ts), then D back into the tile's rows of Ab.
-template <int NT, int W>
-__device__ void update_tc(int ell, const cpx<float> *Jm, Smem<float, W> &sm) {
-  static_assert(W == 32 && NT == 512, "tensor-core update layout");
-  constexpr int TP = W + 1, MT = 128, NN = 64, KC = 16;
-  constexpr uint32_t IDESC = tc::idesc_tf32(MT, NN), LBO = 128, SBO = KC * 32;
-  static_assert(SmemLayout<float, W>::theta_bytes >= size_t(2) * MT * KC * sizeof(float), "A tiles fit");
-  static_assert(SmemLayout<float, W>::ts_bytes >= size_t(2) * NN * KC * sizeof(float), "B tiles fit");
-  float *Ah = reinterpret_cast<float *>(sm.r0), *Al = Ah + MT * KC;
-  float *Bh = reinterpret_cast<float *>(sm.Ts), *Bl = Bh + NN * KC;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int i0 = 0; i0 < ell; i0 += MT) {
-    int chunk = 0;
-    for (int k0 = 0; k0 < 2 * W; k0 += KC, ++chunk) {
-      if (chunk > 0) wait_mma<float, W>(sm);
-      for (int idx = tid; idx < MT * KC; idx += NT) {
-        const int core = idx >> 5, within = idx & 31;
-        const int m = (core / (KC / 4)) * 8 + (within >> 2), k = (core % (KC / 4)) * 4 + (within & 3);
-        const int r = i0 + m, kk = k0 + k;
-        float v = 0.f;
-        if (r < ell) {
-          const cpx<float> x = sm.Ab[r * TP + (kk >> 1)];
-          v = (kk & 1) ? x.y : x.x;
-        }
-        float hi, lo;
-        tc::split_tf32(v, hi, lo);
-        Ah[idx] = hi;
-        Al[idx] = lo;
-      }
-      for (int idx = tid; idx < NN * KC; idx += NT) {
-        const int core = idx >> 5, within = idx & 31;
-        const int n = (core / (KC / 4)) * 8 + (within >> 2), k = (core % (KC / 4)) * 4 + (within & 3);
-        const int kk = k0 + k, a = kk & 1, b = n & 1;
-        const cpx<float> j = Jm[(kk >> 1) * (W + 1) + (n >> 1)];
-        const float v = (a == b) ? j.x : (a == 0 ? j.y : -j.y);
-        float hi, lo;
-        tc::split_tf32(v, hi, lo);
-        Bh[idx] = hi;
-        Bl[idx] = lo;
-      }
-      tc::fence_smem_to_async();
-      __syncthreads();
-      if (tid == 0) {
-        tc::fence_after_sync();
-#pragma unroll
-        for (int st = 0; st < KC / 8; ++st) {
-          const uint32_t off = uint32_t(st) * 2 * LBO;
-          const uint64_t ah = tc::smem_desc(reinterpret_cast<char *>(Ah) + off, LBO, SBO);
-          const uint64_t al = tc::smem_desc(reinterpret_cast<char *>(Al) + off, LBO, SBO);
-          const uint64_t bh = tc::smem_desc(reinterpret_cast<char *>(Bh) + off, LBO, SBO);
-          const uint64_t bl = tc::smem_desc(reinterpret_cast<char *>(Bl) + off, LBO, SBO);
-          tc::mma_tf32(sm.tmem, ah, bh, IDESC, (chunk > 0 || st > 0) ? 1u : 0u);
-          tc::mma_tf32(sm.tmem, ah, bl, IDESC, 1u);
-          tc::mma_tf32(sm.tmem, al, bh, IDESC, 1u);
-        }
-        tc::mma_commit(sm.bar);
-      }
-    }
-    wait_mma<float, W>(sm);
-    tc::fence_after_sync();
-    const int sp = warp & 3, cb = warp >> 2, r = i0 + 32 * sp + lane;
-    float d[16];
-    tc::tmem_ld16(sm.tmem + (uint32_t(32 * sp) << 16) + uint32_t(16 * cb), d);
-    if (r < ell) {
-#pragma unroll
-      for (int j = 0; j < 8; ++j) sm.Ab[r * TP + 8 * cb + j] = mkc<float>(d[2 * j], d[2 * j + 1]);
-    }
-    tc::fence_before_sync();
-    __syncthreads();
-  }
-}
-
 // Rotation of the Hermitian 2x2 [[a, g], [conj g, b]] that zeroes g
 // (Rutishauser's formulas: t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)),
 // zeta = (b - a) / 2|g|, c = 1/sqrt(1 + t^2), s = t c, e = conj(g)/|g|), or
@@ -1138,14 +985,7 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
           dirtyJ = dirtyJ && keepJ;
           resI = bi;
           resJ = bj;
-          if constexpr (sizeof(T) == 4) {
-            if (sm.tc && ell >= 128)
-              gram_tc<NT, W>(ell, sm);
-            else
-              gram_res<T, NT, W>(ell, sm);
-          } else {
-            gram_res<T, NT, W>(ell, sm);
-          }
+          gram_res<T, NT, W>(ell, sm);
         } else {
           gram_stream<T, NT, W>(A, ell, cols, sm);
         }
@@ -1176,14 +1016,7 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
         t1 = t2;
         if constexpr (L::RES_ROWS > 0) {
           if (resident) {
-            if constexpr (sizeof(T) == 4) {
-              if (sm.tc && ell >= 128)
-                update_tc<NT, W>(ell, Jm, sm);
-              else
-                update_res<T, NT, W>(ell, Jm, sm);
-            } else {
-              update_res<T, NT, W>(ell, Jm, sm);
-            }
+            update_res<T, NT, W>(ell, Jm, sm);
             dirtyI = dirtyJ = true;
           } else {
             update_stream<T, NT, W>(A, ell, ell, cols, Jm, sm);
