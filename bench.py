@@ -174,8 +174,8 @@ def measured_peaks():
 
 
 def ncu_traffic():
-    """Per-launch DRAM traffic of the executor kernel from the committed ncu
-    summary (profiles/k_run_traffic.json), scaled by algorithmic bytes."""
+    """DRAM traffic of the executor kernel per algorithmic flop, from the
+    committed ncu summary of a full-size launch (profiles/k_run_traffic.json)."""
     p = ROOT / "profiles" / "k_run_traffic.json"
     if not p.exists():
         return None
@@ -686,7 +686,9 @@ def main():
         "gpu_launches": 3 * a.steps,
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "peak_kind": f"{peaks_kind} bf16 sustained",
-                     "traffic": (tr["bytes_per_launch_scale"] * r["stats"]["bytes"] / a.steps) if tr else None,
+                     "traffic": (tr["bytes_per_flop"] * per_launch) if tr else None,
+                     "traffic_source": "profiles/k_run_traffic.json: DRAM bytes per algorithmic flop of a "
+                                       "full-size launch (ncu), times this launch's flops" if tr else None,
                      "algorithmic_flops_per_launch": per_launch,
                      "simt_fp32": {"peak_tflops_nominal": simt_peak, "frac": achieved / simt_peak},
                      "kernel": "k_run (theta build + Jacobi SVD + truncation + measurement, one CTA per trajectory)"},

@@ -969,6 +969,21 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
         }
         cols[t] = col;
       }
+      // The next cross-block step (I, Jb) keeps block I resident and loads
+      // block Jb: start moving Jb's columns (contiguous, ell values each)
+      // towards L2 now, one 128-byte line per thread, so that the load at the
+      // next step does not wait on HBM.
+      if constexpr (L::RES_ROWS > 0) {
+        if (resident && nblk > 2 && st >= ndiag && st + 1 < nsteps && Jb < nblk) {
+          const int wn = min(B, c - Jb * B);
+          const int lines = (ell * int(sizeof(cpx<T>)) + 127) / 128;
+          for (int idx = threadIdx.x; idx < wn * lines; idx += NT) {
+            const int t = idx / lines, ln = idx - t * lines;
+            const char *ptr = reinterpret_cast<const char *>(A + size_t(ord[Jb * B + t]) * ell) + size_t(ln) * 128;
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(ptr));
+          }
+        }
+      }
       __syncthreads();
       long long t0 = clock64();
       if constexpr (L::RES_ROWS > 0) {
