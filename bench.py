@@ -253,6 +253,23 @@ def cpu_baseline(n, chi, cutoff, layers_by_traj, budget, cores=None):
 
 
 # --------------------------------------------------------------- GPU arm
+def max_over_ranks(x: float, device=None) -> float:
+    """The largest of every rank's value (the timed interval of the slowest
+    rank); the value itself on a single process."""
+    import torch
+    if not (torch.distributed.is_available() and torch.distributed.is_initialized()):
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: int, steps: int, world: int, elapsed_max: float) -> float:
+    """Whole-job throughput: every rank's units over the slowest rank's time
+    (weak scaling: each rank owns its own trajectories)."""
+    return world * units_per_rank * steps / elapsed_max
+
+
 # per-phase SM cycles of the bond operations, counted on the device (one CTA each)
 CYC_KEYS = ("cyc_theta", "cyc_gram", "cyc_rot", "cyc_update", "cyc_final")
 
@@ -334,11 +351,8 @@ def run_gpu(a, rank, world, local_rank):
     elapsed = sum(step_ms) / 1e3
     st = batch.stats(reset=True)
     status = batch.device_status()
-    if world > 1:
-        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed = float(t.item())
-    value = world * B * a.steps / elapsed
+    elapsed = max_over_ranks(elapsed, dev)
+    value = whole_job_rate(B, a.steps, world, elapsed)
     ents = staged[-1]["ents"].cpu().numpy()
 
     # e2e: the C ABI with host buffers (pinned staging, H2D + launch + D2H per step)
@@ -351,16 +365,13 @@ def run_gpu(a, rank, world, local_rank):
     for pk in packs:
         batch.step_packed(pk)
     e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, dev)
     h2d = statistics.mean(int(pk["gates"].nbytes + pk["us"].nbytes + 4 * (pk["gate_ks"].size + pk["meas_ks"].size +
                                                                          2 * B + 2 * (B + 1))) for pk in packs)
     d2h = statistics.mean(int(int(pk["meas_off"][-1]) * (4 + 8) + 8 * B) for pk in packs)
     dims = [batch.bond_dims(i) for i in range(min(B, 5))]
     return dict(value=value, elapsed=elapsed, step_ms=step_ms, split=split, stats=st, status=status, clocks=clk,
-                e2e=world * B * a.steps / e2e_s, h2d=h2d, d2h=d2h, B=B, gpu=name.value.decode(),
+                e2e=whole_job_rate(B, a.steps, world, e2e_s), h2d=h2d, d2h=d2h, B=B, gpu=name.value.decode(),
                 ents=ents, dims=dims, sms=int(sms.value), layer_inputs=layer_inputs)
 
 

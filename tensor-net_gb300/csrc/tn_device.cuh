@@ -1007,7 +1007,12 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
       } else {
         gram_stream<T, NT, W>(A, ell, cols, sm);
       }
-      int need = 0;
+      // Pairs above the threshold, split into pairs inside a half-block and
+      // pairs across the two halves.  A step whose within-half pairs are all
+      // converged rotates only the cross pairs (H rounds instead of W-1), and
+      // vice versa; a sweep still ends only when no pair of any step needs a
+      // rotation, so convergence is decided on every pair as before.
+      int needW = 0, needC = 0;
       for (int idx = threadIdx.x; idx < W * W; idx += NT) {
         int p = idx / W, q = idx % W;
         if (p < q && cols[p] >= 0 && cols[q] >= 0) {
@@ -1016,10 +1021,18 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
           if (mode == 2 && cross) continue;
           T a = sm.G[p * (W + 1) + p].x, b = sm.G[q * (W + 1) + q].x;
           T ag = sqrt(cabs2(sm.G[p * (W + 1) + q]));
-          if (a > tiny2 && b > tiny2 && ag > tol * sqrt(a) * sqrt(b)) need = 1;
+          if (a > tiny2 && b > tiny2 && ag > tol * sqrt(a) * sqrt(b)) {
+            if (cross)
+              needC = 1;
+            else
+              needW = 1;
+          }
         }
       }
-      need = __syncthreads_or(need);
+      needW = __syncthreads_or(needW);
+      needC = __syncthreads_or(needC);
+      const int need = needW | needC;
+      if (mode == 0 && !(needW && needC)) mode = needC ? 1 : 2;
       long long t1 = clock64();
       cyc[0] += t1 - t0;
       cyc[3] += 1;
