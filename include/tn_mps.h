@@ -213,6 +213,16 @@ int tn_batch_step(tn_batch *b, const uint32_t *trajs, uint32_t nt,
                   const uint32_t *meas_off, const uint32_t *meas_ks, const double *us,
                   int32_t *outcomes, double *probs, double *entropy);
 
+/* tn_batch_step with post-selection: posts[j] (parallel to meas_ks) = 0 or 1
+ * projects site meas_ks[j] onto that outcome and reports its Born
+ * probability (Meas::Proj in apply_meas_prob_layer, mps.rs:2236-2242; its
+ * uniform is unused), any other value samples with us[j] (Meas::Rand).
+ * posts = NULL is tn_batch_step. */
+int tn_batch_step_post(tn_batch *b, const uint32_t *trajs, uint32_t nt,
+                       const uint32_t *gate_off, const uint32_t *gate_ks, const double *gates,
+                       const uint32_t *meas_off, const uint32_t *meas_ks, const double *us,
+                       const int32_t *posts, int32_t *outcomes, double *probs, double *entropy);
+
 /* Same layer, inputs already in device memory (pointers from tn_batch_device_inputs);
  * no host copies, no synchronisation (stream-ordered on the batch stream). */
 int tn_batch_device_inputs(tn_batch *b, uint32_t max_gates, uint32_t max_meas,

@@ -346,8 +346,9 @@ class MPS:
 
         ``ks``: target sites (any order, duplicates allowed).  ``us[j]``: the
         uniform for the j-th target after filter/sort/dedup (``Meas::Rand``).
-        ``posts[j]`` (optional, overrides ``us``): a post-selected outcome for
-        that target (``Meas::Proj``, mps.rs:2236-2242).  Returns a list of
+        ``posts[j]`` (optional, overrides ``us[j]``): a post-selected outcome
+        for that target (``Meas::Proj``, mps.rs:2236-2242); ``None`` or a
+        negative entry samples that target (``Meas::Rand``).  Returns a list of
         ``(k, outcome, prob)``.
         """
         targets = sorted(set(int(k) for k in ks if 0 <= int(k) < self.n))
@@ -359,7 +360,7 @@ class MPS:
             if last is not None:
                 for b in range(last, k):
                     self.local_refactor(b)
-            if posts is not None:
+            if posts is not None and posts[j] is not None and int(posts[j]) >= 0:
                 p = int(posts[j])
                 prob = self.local_prob(k, p)
             else:

@@ -9,9 +9,10 @@ This package is the host-side mirror of the reference API over that ABI.
 from . import build
 from ._lib import STATUS, TnError, lib, library_path
 from .batch import Batch
+from .coev import REFERENCE_BONDS, run_coevolution
 from .inputs import gen_layer, gen_trajectory, ginibre, haar_u4
 from .mps import MPS, Trunc
 from .serve import Server, poisson_requests, run_poisson
 
-__all__ = ["MPS", "Trunc", "Batch", "TnError", "STATUS", "lib", "library_path", "build",
+__all__ = ["MPS", "Trunc", "Batch", "run_coevolution", "REFERENCE_BONDS", "TnError", "STATUS", "lib", "library_path", "build",
            "gen_layer", "gen_trajectory", "ginibre", "haar_u4", "Server", "poisson_requests", "run_poisson"]

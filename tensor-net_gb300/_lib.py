@@ -72,6 +72,8 @@ SIGNATURES = {
     "tn_batch_reset": (C.c_int, [vp, u32, u32, P(tn_trunc)]),
     "tn_batch_step": (C.c_int, [vp, P(u32), u32, P(u32), P(u32), P(dbl), P(u32), P(u32), P(dbl),
                                 P(i32), P(dbl), P(dbl)]),
+    "tn_batch_step_post": (C.c_int, [vp, P(u32), u32, P(u32), P(u32), P(dbl), P(u32), P(u32), P(dbl),
+                                     P(i32), P(i32), P(dbl), P(dbl)]),
     "tn_batch_device_inputs": (C.c_int, [vp, u32, u32] + [P(vp)] * 10),
     "tn_batch_step_device": (C.c_int, [vp, u32]),
     "tn_batch_step_ptrs": (C.c_int, [vp, u32] + [vp] * 11),

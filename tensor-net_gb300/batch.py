@@ -61,7 +61,9 @@ class Batch:
             gates=np.ascontiguousarray(np.concatenate(gs).view(np.float64).reshape(-1)) if gs else np.zeros(0),
             meas_off=np.asarray(meas_off, np.uint32), meas_ks=cat(mks, np.uint32), us=cat(uss, np.float64))
 
-    def step_packed(self, pk):
+    def step_packed(self, pk, posts=None):
+        """posts (optional, parallel to pk["meas_ks"]): 0 / 1 post-selects that
+        outcome (Meas::Proj), -1 samples with the uniform (Meas::Rand)."""
         nt = pk["trajs"].size
         nm = int(pk["meas_off"][-1])
         oc = np.zeros(max(nm, 1), np.int32)
@@ -69,19 +71,29 @@ class Batch:
         ent = np.zeros(max(nt, 1), np.float64)
         z = np.zeros(1)
         zu = np.zeros(1, np.uint32)
-        L.check(self._lib.tn_batch_step(
-            self._h, L.uptr(pk["trajs"]), nt, L.uptr(pk["gate_off"]),
-            L.uptr(pk["gate_ks"] if pk["gate_ks"].size else zu),
-            L.dptr(pk["gates"] if pk["gates"].size else z), L.uptr(pk["meas_off"]),
-            L.uptr(pk["meas_ks"] if pk["meas_ks"].size else zu), L.dptr(pk["us"] if pk["us"].size else z),
-            L.iptr(oc), L.dptr(pr), L.dptr(ent)), "tn_batch_step")
+        args = [self._h, L.uptr(pk["trajs"]), nt, L.uptr(pk["gate_off"]),
+                L.uptr(pk["gate_ks"] if pk["gate_ks"].size else zu),
+                L.dptr(pk["gates"] if pk["gates"].size else z), L.uptr(pk["meas_off"]),
+                L.uptr(pk["meas_ks"] if pk["meas_ks"].size else zu), L.dptr(pk["us"] if pk["us"].size else z)]
+        if posts is None:
+            L.check(self._lib.tn_batch_step(*args, L.iptr(oc), L.dptr(pr), L.dptr(ent)), "tn_batch_step")
+        else:
+            ps = np.ascontiguousarray(np.asarray(posts, dtype=np.int32).reshape(-1))
+            assert ps.size == nm
+            zi = np.full(1, -1, np.int32)
+            L.check(self._lib.tn_batch_step_post(*args, L.iptr(ps if ps.size else zi), L.iptr(oc), L.dptr(pr),
+                                                 L.dptr(ent)), "tn_batch_step_post")
         return oc[:nm], pr[:nm], ent[:nt]
 
-    def step(self, trajs, layers):
+    def step(self, trajs, layers, posts=None):
         """Advance each listed trajectory by its layer; returns per-trajectory
-        lists of (k, outcome, prob) and the half-chain entropies."""
+        lists of (k, outcome, prob) and the half-chain entropies.  posts[i]
+        (optional) gives trajectory i's post-selected outcomes, parallel to its
+        sorted measurement sites (-1 = sample)."""
         pk = self.pack(trajs, layers)
-        oc, pr, ent = self.step_packed(pk)
+        flat = None if posts is None else np.concatenate([np.asarray(x, np.int32).reshape(-1) for x in posts]
+                                                         or [np.zeros(0, np.int32)])
+        oc, pr, ent = self.step_packed(pk, flat)
         recs = []
         mo = pk["meas_off"]
         for i in range(len(trajs)):

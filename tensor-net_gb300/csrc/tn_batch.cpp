@@ -104,7 +104,7 @@ namespace {
 
 // Packed per-step layout (same offsets on host and device).
 struct StepLayout {
-  size_t list, order, goff, gks, moff, mks, gates, us, outc, probs, ents, total, in_bytes, out_off;
+  size_t list, order, goff, gks, moff, mks, posts, gates, us, outc, probs, ents, total, in_bytes, out_off;
 };
 
 StepLayout step_layout(uint32_t nt, uint32_t ng, uint32_t nm) {
@@ -123,6 +123,7 @@ StepLayout step_layout(uint32_t nt, uint32_t ng, uint32_t nm) {
   L.gks = take(sizeof(int) * std::max<uint32_t>(ng, 1));
   L.moff = take(sizeof(int) * (nt + 1));
   L.mks = take(sizeof(int) * std::max<uint32_t>(nm, 1));
+  L.posts = take(sizeof(int) * std::max<uint32_t>(nm, 1));
   L.in_bytes = p;
   L.out_off = p;
   L.outc = take(sizeof(int) * std::max<uint32_t>(nm, 1));
@@ -176,6 +177,7 @@ int ensure_step(tn_batch *b, uint32_t nt, uint32_t ng, uint32_t nm) {
 
 struct StepPtrs {
   const int *list, *order, *goff, *gks, *moff, *mks;
+  const int *posts = nullptr;  // per measurement: 0 / 1 post-selected (Meas::Proj), else sampled; null = all sampled
   const double *gates, *us;
   int *outc;
   double *probs, *ents;
@@ -278,9 +280,9 @@ int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P0, bool timed = true)
     CKB(cudaMemsetAsync(b->dcounter, 0, 4 * sizeof(int), b->st));
     CKB(cudaMemsetAsync(b->dcounter + 8, 0, sizeof(int), b->st));
     CKB(cudaMemsetAsync(b->ddyn, 0, sizeof(Item) * nt, b->st));
-    CKB(launch_compile_dd(b->dtraj, P.list, int(nt), P.order, P.goff, P.gks, P.moff, P.mks, b->pcap, b->dprog,
-                          b->ditems, b->dgprog, b->dgitems, b->gcap, b->dcounter + 3, b->dgstart, b->dscratch,
-                          b->drem, b->ddyn, b->dcounter + 8, b->st));
+    CKB(launch_compile_dd(b->dtraj, P.list, int(nt), P.order, P.goff, P.gks, P.moff, P.mks, P.posts, b->pcap,
+                          b->dprog, b->ditems, b->dgprog, b->dgitems, b->gcap, b->dcounter + 3, b->dgstart,
+                          b->dscratch, b->drem, b->ddyn, b->dcounter + 8, b->st));
     la.counter = b->dcounter;
     la.items = b->dgitems;
     la.nitems = 0;
@@ -303,8 +305,8 @@ int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P0, bool timed = true)
     }
     return TN_OK;
   }
-  CKB(launch_compile(b->dtraj, P.list, int(nt), P.order, P.goff, P.gks, P.moff, P.mks, b->pcap, b->dprog, b->ditems,
-                     b->dgprog, b->dgitems, b->gcap, b->dcounter + 3, b->st));
+  CKB(launch_compile(b->dtraj, P.list, int(nt), P.order, P.goff, P.gks, P.moff, P.mks, P.posts, b->pcap, b->dprog,
+                     b->ditems, b->dgprog, b->dgitems, b->gcap, b->dcounter + 3, b->st));
   CKB(cudaMemsetAsync(b->dcounter, 0, 3 * sizeof(int), b->st));
   la.counter = b->dcounter;
   // launch 1: every gate of the layer is an independent item
@@ -495,6 +497,14 @@ int tn_batch_reset(tn_batch *b, uint32_t t, uint32_t n, const tn_trunc *trunc) {
 int tn_batch_step(tn_batch *b, const uint32_t *trajs, uint32_t nt, const uint32_t *gate_off, const uint32_t *gate_ks,
                   const double *gates, const uint32_t *meas_off, const uint32_t *meas_ks, const double *us,
                   int32_t *outcomes, double *probs, double *entropy) {
+  return tn_batch_step_post(b, trajs, nt, gate_off, gate_ks, gates, meas_off, meas_ks, us, nullptr, outcomes, probs,
+                            entropy);
+}
+
+int tn_batch_step_post(tn_batch *b, const uint32_t *trajs, uint32_t nt, const uint32_t *gate_off,
+                       const uint32_t *gate_ks, const double *gates, const uint32_t *meas_off,
+                       const uint32_t *meas_ks, const double *us, const int32_t *posts, int32_t *outcomes,
+                       double *probs, double *entropy) {
   if (!b || !trajs || !gate_off || !meas_off) return TN_ERR_INVALID_ARG;
   if (nt == 0) return TN_OK;
   const uint32_t ng = gate_off[nt], nm = meas_off[nt];
@@ -535,10 +545,12 @@ int tn_batch_step(tn_batch *b, const uint32_t *trajs, uint32_t nt, const uint32_
   for (uint32_t j = 0; j < nm; ++j) mk[j] = int(meas_ks[j]);
   if (ng) std::memcpy(hb + L.gates, gates, sizeof(double) * 32 * ng);
   if (nm) std::memcpy(hb + L.us, us, sizeof(double) * nm);
+  if (posts && nm) std::memcpy(hb + L.posts, posts, sizeof(int) * nm);
   if (int s = tune_before(b)) return s;
   CKB(cudaMemcpyAsync(b->dstep, b->hstep, L.in_bytes, cudaMemcpyHostToDevice, b->st));
   StepPtrs P = ptrs_of(L, reinterpret_cast<char *>(b->dstep));
   P.order = nullptr;  // ranked on the device from the current bond dimensions
+  P.posts = posts ? reinterpret_cast<const int *>(reinterpret_cast<char *>(b->dstep) + L.posts) : nullptr;
   if (int s = launch_step(b, nt, P)) return s;
   const size_t out_bytes = L.total - L.out_off;
   CKB(cudaMemcpyAsync(hb + L.out_off, reinterpret_cast<char *>(b->dstep) + L.out_off, out_bytes,

@@ -114,9 +114,11 @@ size_t run_smem_bytes(int prec, int sortP);
 size_t run_work_bytes(int prec, int cap);
 int run_blocks_per_sm(int prec, int sortP);
 cudaError_t launch_reset(TrajDev *trajs, const int *list, int count, int prec, cudaStream_t st);
+// posts (may be null): per measurement, 0 / 1 = post-selected outcome (Meas::Proj), else sampled
 cudaError_t launch_compile(const TrajDev *trajs, const int *list, int nt, const int *order, const int *gate_off,
-                           const int *gate_ks, const int *meas_off, const int *meas_ks, int pcap, Instr *prog,
-                           Item *items, Instr *gprog, Item *gitems, int gcap, int *gcount, cudaStream_t st);
+                           const int *gate_ks, const int *meas_off, const int *meas_ks, const int *posts, int pcap,
+                           Instr *prog, Item *items, Instr *gprog, Item *gitems, int gcap, int *gcount,
+                           cudaStream_t st);
 // order[i] = execution rank of listed trajectory i, most expensive first by
 // the current bond dimensions (a single-block sort on the device).
 cudaError_t launch_lpt_order(const TrajDev *trajs, const int *list, int nt, const int *meas_off, int *order,
@@ -126,9 +128,9 @@ cudaError_t launch_lpt_order(const TrajDev *trajs, const int *list, int nt, cons
 // programs at sweeps[i], rem[i] = gate items of trajectory i, and trajectories
 // without gate items pushed at once.
 cudaError_t launch_compile_dd(const TrajDev *trajs, const int *list, int nt, const int *order, const int *gate_off,
-                              const int *gate_ks, const int *meas_off, const int *meas_ks, int pcap, Instr *prog,
-                              Item *sweeps, Instr *gprog, Item *gitems, int gcap, int *gcount, int *gstart,
-                              int *scratch, int *rem, Item *dyn, int *dyn_tail, cudaStream_t st);
+                              const int *gate_ks, const int *meas_off, const int *meas_ks, const int *posts, int pcap,
+                              Instr *prog, Item *sweeps, Instr *gprog, Item *gitems, int gcap, int *gcount,
+                              int *gstart, int *scratch, int *rem, Item *dyn, int *dyn_tail, cudaStream_t st);
 
 // Device-side view of a single-state handle (for entry points outside
 // tn_host.cpp that launch on it).

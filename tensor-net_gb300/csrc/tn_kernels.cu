@@ -152,8 +152,8 @@ __global__ void k_reset(TrajDev *trajs, const int *list, int count, int elem_byt
 // first.  A trajectory whose gates overlap keeps them, in order, at the head
 // of its second-launch program instead.
 __global__ void k_compile(const TrajDev *trajs, const int *list, int nt, const int *order, const int *gate_off,
-                          const int *gate_ks, const int *meas_off, const int *meas_ks, int pcap, Instr *prog,
-                          Item *items, Instr *gprog, Item *gitems, int gcap, int *gcount) {
+                          const int *gate_ks, const int *meas_off, const int *meas_ks, const int *posts, int pcap,
+                          Instr *prog, Item *items, Instr *gprog, Item *gitems, int gcap, int *gcount) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) *gcount = min(gate_off[nt], gcap);
   if (i >= nt) return;
@@ -191,7 +191,7 @@ __global__ void k_compile(const TrajDev *trajs, const int *list, int nt, const i
     if (k < 0 || k >= n || k <= last) continue;  // host guarantees sorted unique
     if (last >= 0)
       for (int b = last; b < k; ++b) emit(OP_REFACTOR, b, 0, 0);
-    emit(OP_MEAS, k, j, -1);
+    emit(OP_MEAS, k, j, posts ? (posts[j] == 0 || posts[j] == 1 ? posts[j] : -1) : -1);
     last = k;
   }
   if (last >= 0) {
@@ -305,7 +305,8 @@ __global__ void k_gate_slots(int nt, const int *order, const int *gate_off, int 
 // sweeps[i], rem[i] = number of gate items of trajectory i; a trajectory
 // without gate items has its sweep item pushed here.
 __global__ void k_compile_dd(const TrajDev *trajs, const int *list, int nt, const int *gate_off, const int *gate_ks,
-                             const int *meas_off, const int *meas_ks, int pcap, Instr *prog, Item *sweeps,
+                             const int *meas_off, const int *meas_ks, const int *posts, int pcap, Instr *prog,
+                             Item *sweeps,
                              Instr *gprog, Item *gitems, int gcap, int *gcount, const int *gstart, int *rem, Item *dyn,
                              int *dyn_tail) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -348,7 +349,7 @@ __global__ void k_compile_dd(const TrajDev *trajs, const int *list, int nt, cons
     if (k < 0 || k >= n || k <= last) continue;  // host guarantees sorted unique
     if (last >= 0)
       for (int b = last; b < k; ++b) emit(OP_REFACTOR, b, 0, 0);
-    emit(OP_MEAS, k, j, -1);
+    emit(OP_MEAS, k, j, posts ? (posts[j] == 0 || posts[j] == 1 ? posts[j] : -1) : -1);
     last = k;
   }
   if (last >= 0) {
@@ -429,11 +430,12 @@ cudaError_t launch_reset(TrajDev *trajs, const int *list, int count, int prec, c
 }
 
 cudaError_t launch_compile(const TrajDev *trajs, const int *list, int nt, const int *order, const int *gate_off,
-                           const int *gate_ks, const int *meas_off, const int *meas_ks, int pcap, Instr *prog,
-                           Item *items, Instr *gprog, Item *gitems, int gcap, int *gcount, cudaStream_t st) {
+                           const int *gate_ks, const int *meas_off, const int *meas_ks, const int *posts, int pcap,
+                           Instr *prog, Item *items, Instr *gprog, Item *gitems, int gcap, int *gcount,
+                           cudaStream_t st) {
   if (nt <= 0) return cudaSuccess;
-  k_compile<<<(nt + 127) / 128, 128, 0, st>>>(trajs, list, nt, order, gate_off, gate_ks, meas_off, meas_ks, pcap,
-                                              prog, items, gprog, gitems, gcap, gcount);
+  k_compile<<<(nt + 127) / 128, 128, 0, st>>>(trajs, list, nt, order, gate_off, gate_ks, meas_off, meas_ks, posts,
+                                              pcap, prog, items, gprog, gitems, gcap, gcount);
   return cudaGetLastError();
 }
 
@@ -447,13 +449,14 @@ cudaError_t launch_lpt_order(const TrajDev *trajs, const int *list, int nt, cons
 }
 
 cudaError_t launch_compile_dd(const TrajDev *trajs, const int *list, int nt, const int *order, const int *gate_off,
-                              const int *gate_ks, const int *meas_off, const int *meas_ks, int pcap, Instr *prog,
-                              Item *sweeps, Instr *gprog, Item *gitems, int gcap, int *gcount, int *gstart,
-                              int *scratch, int *rem, Item *dyn, int *dyn_tail, cudaStream_t st) {
+                              const int *gate_ks, const int *meas_off, const int *meas_ks, const int *posts, int pcap,
+                              Instr *prog, Item *sweeps, Instr *gprog, Item *gitems, int gcap, int *gcount,
+                              int *gstart, int *scratch, int *rem, Item *dyn, int *dyn_tail, cudaStream_t st) {
   if (nt <= 0) return cudaSuccess;
   k_gate_slots<<<1, 1024, 0, st>>>(nt, order, gate_off, scratch, gstart);
-  k_compile_dd<<<(nt + 127) / 128, 128, 0, st>>>(trajs, list, nt, gate_off, gate_ks, meas_off, meas_ks, pcap, prog,
-                                                 sweeps, gprog, gitems, gcap, gcount, gstart, rem, dyn, dyn_tail);
+  k_compile_dd<<<(nt + 127) / 128, 128, 0, st>>>(trajs, list, nt, gate_off, gate_ks, meas_off, meas_ks, posts, pcap,
+                                                 prog, sweeps, gprog, gitems, gcap, gcount, gstart, rem, dyn,
+                                                 dyn_tail);
   return cudaGetLastError();
 }
 

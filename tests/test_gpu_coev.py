@@ -1,0 +1,57 @@
+"""Batched post-selection (Meas::Proj, mps.rs:2236-2242) and the multi-chi
+coevolution replay (haar_coev_probs.rs:34-80) against the FP64 oracle on the
+same circuit, uniforms and recorded outcomes."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_batch_post_selection_matches_oracle(pkg, ref):
+    n, chi = 8, 8
+    b = pkg.Batch([n, n], [pkg.Trunc.const(chi)] * 2, "f64")
+    r0, r1 = ref.MPS(n, ref.Trunc.const(chi)), ref.MPS(n, ref.Trunc.const(chi))
+    for t in range(8):
+        gk, g, mk, us = pkg.gen_layer(3, 0, t, n, 0.4)
+        posts = [np.array([(t + j) % 2 for j in range(len(mk))], np.int32),   # all post-selected
+                 np.array([-1 if j % 2 else 1 for j in range(len(mk))], np.int32)]  # mixed
+        recs, ents = b.step([0, 1], [(gk, g, mk, us)] * 2, posts=posts)
+        for m, ps, rec in ((r0, posts[0], recs[0]), (r1, posts[1], recs[1])):
+            for k, op in zip(gk, g):
+                m.apply_unitary2(int(k), op)
+            want = m.apply_meas_prob_layer(mk, us, posts=[int(x) if x >= 0 else None for x in ps])
+            assert [x[:2] for x in rec] == [x[:2] for x in want]
+            np.testing.assert_allclose([x[2] for x in rec], [x[2] for x in want], atol=1e-9)
+            for j, x in enumerate(ps):
+                if x >= 0:
+                    assert rec[j][1] == x
+        np.testing.assert_allclose(ents, [r0.entropy_vn(n // 2 - 1), r1.entropy_vn(n // 2 - 1)], atol=1e-9)
+    assert b.device_status() == 0
+
+
+def test_coevolution_replay_matches_oracle(pkg, ref):
+    n, depth, p, runs, seed = 8, 6, 0.3, 2, 21
+    bonds = (2, 4, None)
+    out = pkg.run_coevolution(n, depth, p, runs, seed, bonds=bonds, precision="f64")
+    assert out["device_status"] == (0, 0)
+    M = out["sites"].shape[0]
+    assert out["outcomes"].shape == (runs, M) and out["probs"].shape == (runs, len(bonds), M)
+    from tensor_net_gb300.coev import run_uniforms
+    for r in range(runs):
+        samp = ref.MPS(n, ref.Trunc.none())
+        reps = [ref.MPS(n, ref.Trunc.const(c)) for c in bonds[:-1]]
+        col = 0
+        for t in range(depth):
+            gk, g, mk, _ = pkg.gen_layer(seed, 0, t, n, p)
+            us = run_uniforms(seed, r, t, len(mk))
+            rec = ref.apply_bilayer(samp, gk, g, mk, us)
+            outs = [o for (_, o, _) in rec]
+            np.testing.assert_array_equal(out["outcomes"][r, col:col + len(mk)], outs)
+            np.testing.assert_allclose(out["probs"][r, -1, col:col + len(mk)], [q for (_, _, q) in rec], atol=1e-9)
+            for ci, m in enumerate(reps):
+                for k, op in zip(gk, g):
+                    m.apply_unitary2(int(k), op)
+                rr = m.apply_meas_prob_layer(mk, np.zeros(len(mk)), posts=outs)
+                np.testing.assert_allclose(out["probs"][r, ci, col:col + len(mk)], [q for (_, _, q) in rr],
+                                           atol=1e-9)
+            col += len(mk)
