@@ -58,7 +58,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--schedule", type=int, default=1, choices=[0, 1])
-    ap.add_argument("--workload", default="batch", choices=["batch", "mixed", "large", "precision"],
+    ap.add_argument("--runs", type=int, default=64, help="coev: sampled trajectories")
+    ap.add_argument("--workload", default="batch", choices=["batch", "mixed", "large", "precision", "coev"],
                     help="batch: the headline line; mixed: the batching workload; large: n=128, chi_max=1024; "
                          "precision: mixed vs float64 errors per p (uses --n, --chi, --depth)")
     ap.add_argument("--depth", type=int, default=64)
@@ -555,6 +556,24 @@ def run_large(a):
             "unit": "s per layer"}
 
 
+def run_coev(a):
+    """The multi-chi coevolution replay (the reference's production driver,
+    workspace/src/haar_coev_probs.rs): `--runs` sampled trajectories of one
+    circuit without truncation, each replayed at the reference's 15 chi_max
+    values with post-selected outcomes; n = --n, depth = --depth, p = 0.1."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    t0 = time.perf_counter()
+    out = pkg.run_coevolution(a.n, a.depth, 0.1, a.runs, a.seed, precision=a.prec)
+    wall = time.perf_counter() - t0
+    trajs = a.runs * len(pkg.REFERENCE_BONDS)
+    return {"workload": f"coevolution replay: n={a.n} depth={a.depth} p=0.1, {a.runs} runs x "
+                        f"{len(pkg.REFERENCE_BONDS)} chi_max (4..72 and untruncated), host-driven layer steps",
+            "trajectories": trajs, "value": trajs * a.depth / wall, "unit": UNIT, "wall_s": wall,
+            "measurements_per_run": int(out["sites"].shape[0]), "device_status": list(out["device_status"]),
+            "precision": a.prec}
+
+
 def run_precision(a):
     """Errors of the mixed path against the float64 GPU path (itself held to
     the FP64 oracle by the parity tests) on identical inputs: per p of the
@@ -662,12 +681,12 @@ def main():
         print(json.dumps(out), flush=True)
         return
 
-    if a.workload in ("mixed", "large", "precision"):
+    if a.workload in ("mixed", "large", "precision", "coev"):
         if rank != 0:
             return
         import torch
         torch.cuda.set_device(0)
-        out = {"mixed": run_mixed, "large": run_large, "precision": run_precision}[a.workload](a)
+        out = {"mixed": run_mixed, "large": run_large, "precision": run_precision, "coev": run_coev}[a.workload](a)
         out.update({"metric": METRIC if a.workload == "mixed" else "per-layer time and entropy",
                     "n_gpus": 1, "data": "synthetic (seeded Haar gates and measurement uniforms)"})
         print(json.dumps(out), flush=True)
