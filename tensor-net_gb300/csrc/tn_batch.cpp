@@ -82,7 +82,7 @@ struct tn_batch {
   int gcap = 0;
   uint32_t sum_n = 0;
   // [0] queue head, [1] reset list, [2] second-launch queue, [3] gate count, [4..8) bind staging,
-  // [8] push counter, [9] queue-wait error
+  // [8] push counter, [9] queue-wait error, [10] sweep head
   int *dcounter = nullptr;
   int schedule = 1;  // 1: one launch per layer, sweeps pushed as gates finish; 0: two launches
   int *drem = nullptr, *dgstart = nullptr, *dscratch = nullptr, *dorder = nullptr;
@@ -278,7 +278,7 @@ int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P0, bool timed = true)
     // One launch: gate items (most expensive trajectories first), then each
     // trajectory's sweep program as soon as its last gate item has finished.
     CKB(cudaMemsetAsync(b->dcounter, 0, 4 * sizeof(int), b->st));
-    CKB(cudaMemsetAsync(b->dcounter + 8, 0, sizeof(int), b->st));
+    CKB(cudaMemsetAsync(b->dcounter + 8, 0, 3 * sizeof(int), b->st));  // push tail, queue error, sweep head
     CKB(cudaMemsetAsync(b->ddyn, 0, sizeof(Item) * nt, b->st));
     CKB(launch_compile_dd(b->dtraj, P.list, int(nt), P.order, P.goff, P.gks, P.moff, P.mks, P.posts, b->pcap,
                           b->dprog, b->ditems, b->dgprog, b->dgitems, b->gcap, b->dcounter + 3, b->dgstart,
@@ -293,6 +293,7 @@ int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P0, bool timed = true)
     la.sweeps = b->ditems;
     la.dyn = b->ddyn;
     la.dyn_tail = b->dcounter + 8;
+    la.dyn_head = b->dcounter + 10;
     la.nsweeps = int(nt);
     if (timed) CKB(cudaEventRecord(b->ev[0], b->st));
     CKB(launch_run(b->prec, la, gmax, b->sortP, b->maxcap, b->st));

@@ -102,6 +102,7 @@ struct LaunchArgs {
   const Item *sweeps;     // per listed trajectory: measurement layer + sweep + entropy program
   Item *dyn;              // pushed sweep items (aux = 1 once written); zeroed before compile
   int *dyn_tail;          // push counter; zeroed before compile
+  int *dyn_head;          // sweep slots claimed; zeroed before the launch
   int nsweeps;
   int *qerr;              // set to 1 when a queue wait ran past its time limit
 };

@@ -37,10 +37,12 @@ __device__ void push_sweep(Item *dyn, int *tail, const Item *sweeps, int i) {
 }
 
 // Static schedule (la.rem == nullptr): items[0, count) in counter order.
-// Dependency-driven schedule: gate items first; a CTA that pulls an index
-// past them waits (bounded by kQueueWaitNs) for the matching pushed sweep
-// item.  Every pushed item depends only on items already pulled by running
-// CTAs, so the waits end; a wait that runs out sets qerr and the CTA moves on.
+// Dependency-driven schedule: a CTA takes a pushed sweep item when one is
+// ready (claimed by compare-and-swap on the sweep head below the push tail),
+// else the next gate item; once the gate items are gone it claims the next
+// sweep slot and waits (bounded by kQueueWaitNs) for its push.  Every pushed
+// item depends only on gate items already taken by running CTAs, so the
+// waits end; a wait that runs out sets qerr and the CTA moves on.
 template <typename T, int NT, int W>
 __global__ void __launch_bounds__(NT, 1) k_run(LaunchArgs la, int sortP, int ws_cap) {
   extern __shared__ __align__(256) unsigned char smem[];
@@ -73,14 +75,35 @@ __global__ void __launch_bounds__(NT, 1) k_run(LaunchArgs la, int sortP, int ws_
   }
   for (;;) {
     if (threadIdx.x == 0) {
-      const int it = atomicAdd(la.counter, 1);
       const int G = la.nitems_dev ? *la.nitems_dev : la.nitems;
-      int kind = 0;
-      if (it < G) {
-        s_item = la.items[it];
-        kind = 1;
-      } else if (dd && it < G + la.nsweeps) {
-        Item *slot = la.dyn + (it - G);
+      int kind = 0, slot_i = -1;
+      if (dd) {
+        // A pushed sweep item that is already there goes first: the sweeps
+        // are the serial chains that bound the launch, the gate items are
+        // independent filler.
+        int h = *reinterpret_cast<volatile int *>(la.dyn_head);
+        while (h < *reinterpret_cast<volatile int *>(la.dyn_tail)) {
+          const int prev = atomicCAS(la.dyn_head, h, h + 1);
+          if (prev == h) {
+            slot_i = h;
+            break;
+          }
+          h = prev;
+        }
+      }
+      if (slot_i < 0) {
+        const int it = atomicAdd(la.counter, 1);
+        if (it < G) {
+          s_item = la.items[it];
+          kind = 1;
+        } else if (dd) {
+          // no gate left: claim the next sweep slot and wait for its push
+          const int h = atomicAdd(la.dyn_head, 1);
+          if (h < la.nsweeps) slot_i = h;
+        }
+      }
+      if (slot_i >= 0) {
+        Item *slot = la.dyn + slot_i;
         const unsigned long long t0 = global_ns();
         kind = 2;
         while (load_acquire(&slot->aux) == 0) {
