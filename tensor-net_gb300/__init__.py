@@ -8,6 +8,7 @@ This package is the host-side mirror of the reference API over that ABI.
 """
 from . import build
 from ._lib import STATUS, TnError, lib, library_path
+from . import circuits
 from .batch import Batch
 from .coev import REFERENCE_BONDS, run_coevolution
 from .inputs import gen_layer, gen_trajectory, ginibre, haar_u4
