@@ -165,7 +165,10 @@ template <typename T, int W>
 struct SmemLayout {
   static constexpr int TU = 16;
   static constexpr int TILE = 32;                 // theta tile: 32 (v) x 32 (w)
-  static constexpr int TP = W + 1;                // padded row pitch of Ts / Ab
+  static constexpr int TP = W + 1;                // padded row pitch of Ts
+  // row pitch of the resident block Ab: even for float, so that a row starts
+  // on a 16-byte boundary and the Gram's broadcast reads are 16 bytes wide
+  static constexpr int AP = sizeof(T) == 4 ? W + 2 : W + 1;
   static constexpr int RES_ROWS = sizeof(T) == 4 ? 512 : 0;
   static constexpr int GK = 16, GT = 64;          // recovery GEMM: K chunk, 64x64 tile
   static constexpr size_t theta_bytes = size_t(2) * TILE * 2 * TU * sizeof(cpx<T>);
@@ -176,7 +179,7 @@ struct SmemLayout {
     size_t r = g > s ? g : s;
     return (r + 255) & ~size_t(255);
   }
-  static constexpr size_t ab_bytes = size_t(RES_ROWS) * TP * sizeof(cpx<T>);
+  static constexpr size_t ab_bytes = size_t(RES_ROWS) * AP * sizeof(cpx<T>);
   static constexpr int GP = W + 1;                // padded row pitch of G and J
   static constexpr size_t g_bytes = size_t(W) * GP * sizeof(cpx<T>);
   static constexpr size_t ts_bytes = size_t(32) * TP * sizeof(cpx<T>);
@@ -640,7 +643,7 @@ __device__ void update_stream(cpx<T> *__restrict__ X, int ld, int rows, const in
 // back to A; eight independent accesses in flight per thread.  No barrier.
 template <typename T, int NT, int W>
 __device__ void load_half_res(const cpx<T> *__restrict__ A, int ell, const int *rc, int s0, Smem<T, W> &sm) {
-  constexpr int TP = W + 1, B = W / 2, UN = 8;
+  constexpr int TP = SmemLayout<T, W>::AP, B = W / 2, UN = 8;
   const int tot = B * ell;
   for (int base = threadIdx.x; base < tot; base += NT * UN) {
     cpx<T> v[UN];
@@ -661,7 +664,7 @@ __device__ void load_half_res(const cpx<T> *__restrict__ A, int ell, const int *
 
 template <typename T, int NT, int W>
 __device__ void store_half_res(cpx<T> *__restrict__ A, int ell, const int *rc, int s0, const Smem<T, W> &sm) {
-  constexpr int TP = W + 1, B = W / 2;
+  constexpr int TP = SmemLayout<T, W>::AP, B = W / 2;
   for (int idx = threadIdx.x; idx < B * ell; idx += NT) {
     const int p = idx / ell, r = idx - p * ell;
     if (rc[s0 + p] >= 0) A[size_t(rc[s0 + p]) * ell + r] = sm.Ab[r * TP + s0 + p];
@@ -677,7 +680,8 @@ template <typename T, int NT, int W>
 __device__ void gram_res(int ell, Smem<T, W> &sm) {
   static_assert(W == 32 && NT == 512, "resident Gram assumes W = 32, 16 warps");
   static_assert(SmemLayout<T, W>::theta_bytes >= 2 * W * W * sizeof(cpx<T>), "partials fit region 0");
-  constexpr int TP = W + 1, GP = W + 1, RS = 8, KS = 4;
+  constexpr int TP = SmemLayout<T, W>::AP, GP = W + 1, RS = 8, KS = 4;
+  static_assert(TP % 2 == 0, "16-byte aligned rows");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int p0 = RS * (warp % KS), ks = warp / KS;
   cpx<T> acc[RS];
@@ -687,10 +691,15 @@ __device__ void gram_res(int ell, Smem<T, W> &sm) {
   for (; r + KS < ell; r += 2 * KS) {
     const cpx<T> *row0 = sm.Ab + r * TP, *row1 = row0 + KS * TP;
     cpx<T> x0[RS], x1[RS];
+    // eight consecutive complex values of each row as four 16-byte broadcasts
+    const float4 *v0 = reinterpret_cast<const float4 *>(row0 + p0), *v1 = reinterpret_cast<const float4 *>(row1 + p0);
 #pragma unroll
-    for (int i = 0; i < RS; ++i) {
-      x0[i] = row0[p0 + i];
-      x1[i] = row1[p0 + i];
+    for (int i = 0; i < RS / 2; ++i) {
+      const float4 a = v0[i], b = v1[i];
+      x0[2 * i] = mkc<T>(a.x, a.y);
+      x0[2 * i + 1] = mkc<T>(a.z, a.w);
+      x1[2 * i] = mkc<T>(b.x, b.y);
+      x1[2 * i + 1] = mkc<T>(b.z, b.w);
     }
     const cpx<T> y0 = row0[lane], y1 = row1[lane];
 #pragma unroll
@@ -721,7 +730,7 @@ __device__ void gram_res(int ell, Smem<T, W> &sm) {
 template <typename T, int NT, int W>
 __device__ void update_res(int ell, const cpx<T> *__restrict__ Jm, Smem<T, W> &sm) {
   static_assert(W == 32 && NT % 4 == 0, "resident update layout");
-  constexpr int TP = W + 1, RB = NT / 4;
+  constexpr int TP = SmemLayout<T, W>::AP, RB = NT / 4;
   static_assert(SmemLayout<T, W>::RES_ROWS <= 4 * RB, "one pass covers every resident row");
   const int qb = threadIdx.x / RB, rb = threadIdx.x % RB;
   const int q0 = qb * 8;
