@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--schedule", type=int, default=1, choices=[0, 1])
     ap.add_argument("--runs", type=int, default=64, help="coev: sampled trajectories")
-    ap.add_argument("--workload", default="batch", choices=["batch", "mixed", "large", "precision", "coev"],
+    ap.add_argument("--workload", default="batch", choices=["batch", "mixed", "large", "precision", "coev", "plain"],
                     help="batch: the headline line; mixed: the batching workload; large: n=128, chi_max=1024; "
                          "precision: mixed vs float64 errors per p (uses --n, --chi, --depth)")
     ap.add_argument("--depth", type=int, default=64)
@@ -556,6 +556,49 @@ def run_large(a):
             "unit": "s per layer"}
 
 
+def run_plain_small(a):
+    """The plain-method workload (N=16, depth 32, p=0.1, chi_max=64, cutoff
+    1e-12): one trajectory through the single-state API in float64 on the
+    GPU, and the FP64 oracle on one host core, on the same inputs; traj-layers
+    per second for each and the largest entropy difference."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    sys.path.insert(0, str(ROOT))
+    from oracle import mps_ref as R
+    n, depth, p, chi, cut = 16, 32, 0.1, 64, 1e-12
+    trajs = [pkg.gen_trajectory(a.seed, i, n, depth, p) for i in range(4)]
+    m = pkg.MPS.new_qubits(n, pkg.Trunc.both(chi, cut), "f64")
+    for L_ in trajs[0][:2]:
+        m.apply_bilayer(*L_)  # warm-up (module load, first launches)
+    m.close()
+    g_ents, t0 = [], time.perf_counter()
+    for tr in trajs:
+        m = pkg.MPS.new_qubits(n, pkg.Trunc.both(chi, cut), "f64")
+        e = []
+        for L_ in tr:
+            m.apply_bilayer(*L_)
+            e.append(m.entropy_vn(n // 2 - 1))
+        g_ents.append(e)
+        m.close()
+    g_s = time.perf_counter() - t0
+    c_ents, t0 = [], time.perf_counter()
+    for tr in trajs:
+        r = R.MPS(n, R.Trunc.both(chi, cut))
+        e = []
+        for L_ in tr:
+            R.apply_bilayer(r, *L_)
+            e.append(r.entropy_vn(n // 2 - 1))
+        c_ents.append(e)
+    c_s = time.perf_counter() - t0
+    err = max(abs(x - y) for ge_, ce in zip(g_ents, c_ents) for x, y in zip(ge_, ce))
+    units = len(trajs) * depth
+    return {"workload": f"plain method: N={n} depth={depth} p={p} chi_max={chi} cutoff={cut:g}, "
+                        f"{len(trajs)} trajectories one at a time",
+            "gpu_plain_f64": {"value": units / g_s, "unit": UNIT},
+            "cpu_oracle_1core": {"value": units / c_s, "unit": UNIT},
+            "entropy_abs_max_vs_oracle": err}
+
+
 def run_coev(a):
     """The multi-chi coevolution replay (the reference's production driver,
     workspace/src/haar_coev_probs.rs): `--runs` sampled trajectories of one
@@ -681,12 +724,13 @@ def main():
         print(json.dumps(out), flush=True)
         return
 
-    if a.workload in ("mixed", "large", "precision", "coev"):
+    if a.workload in ("mixed", "large", "precision", "coev", "plain"):
         if rank != 0:
             return
         import torch
         torch.cuda.set_device(0)
-        out = {"mixed": run_mixed, "large": run_large, "precision": run_precision, "coev": run_coev}[a.workload](a)
+        out = {"mixed": run_mixed, "large": run_large, "precision": run_precision, "coev": run_coev,
+               "plain": run_plain_small}[a.workload](a)
         out.update({"metric": METRIC if a.workload == "mixed" else "per-layer time and entropy",
                     "n_gpus": 1, "data": "synthetic (seeded Haar gates and measurement uniforms)"})
         print(json.dumps(out), flush=True)
