@@ -59,7 +59,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--schedule", type=int, default=1, choices=[0, 1])
     ap.add_argument("--runs", type=int, default=64, help="coev: sampled trajectories")
-    ap.add_argument("--workload", default="batch", choices=["batch", "mixed", "large", "precision", "coev", "plain"],
+    ap.add_argument("--workload", default="batch", choices=["batch", "mixed", "large", "precision", "coev", "plain",
+                                                                 "f64"],
                     help="batch: the headline line; mixed: the batching workload; large: n=128, chi_max=1024; "
                          "precision: mixed vs float64 errors per p (uses --n, --chi, --depth)")
     ap.add_argument("--depth", type=int, default=64)
@@ -599,6 +600,45 @@ def run_plain_small(a):
             "entropy_abs_max_vs_oracle": err}
 
 
+def run_f64(a):
+    """The headline workload (N=64, chi_max=256, p cycling) in float64 -- the
+    mode that meets the 1e-6 entropy bound (errors ~1e-14 against the oracle)
+    -- batched vs plain on one timed layer: `--batch` trajectories after
+    `--prefill` layers (one warm-up layer), and one trajectory (p=0.10)
+    through the single-state API on the same layer."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    n, chi, B = a.n, a.chi, a.batch
+    trunc = pkg.Trunc.both(chi, a.cutoff)
+    batch = pkg.Batch([n] * B, [trunc] * B, "f64")
+    trajs = list(range(B))
+    lay = lambda t: [pkg.gen_layer(a.seed, i, t, n, p_of(i)) for i in trajs]
+    for t in range(a.prefill + 1):
+        batch.step(trajs, lay(t))
+    batch.synchronize()
+    t_lo = a.prefill + 1
+    pk = batch.pack(trajs, lay(t_lo))
+    t0 = time.perf_counter()
+    batch.step_packed(pk)
+    b_s = time.perf_counter() - t0
+    st = batch.stats(reset=True)
+    batch.close()
+    m = pkg.MPS.new_qubits(n, trunc, "f64")
+    for t in range(t_lo):
+        m.apply_bilayer(*pkg.gen_layer(a.seed, 1, t, n, p_of(1)))
+    t0 = time.perf_counter()
+    m.apply_bilayer(*pkg.gen_layer(a.seed, 1, t_lo, n, p_of(1)))
+    m.entropy_vn(n // 2 - 1)
+    p_s = time.perf_counter() - t0
+    m.close()
+    return {"workload": f"N={n} chi_max={chi} float64, {B} trajectories, layer {t_lo} after {a.prefill + 1}",
+            "batched_f64": {"value": B / b_s, "unit": UNIT, "layer_s": b_s},
+            "plain_f64_p0.10": {"value": 1.0 / p_s, "unit": UNIT, "layer_s": p_s},
+            "batched_over_plain": (B / b_s) * p_s,
+            "note": "host-timed, inputs through tn_batch_step (e2e); plain = one p=0.10 trajectory"}
+
+
 def run_coev(a):
     """The multi-chi coevolution replay (the reference's production driver,
     workspace/src/haar_coev_probs.rs): `--runs` sampled trajectories of one
@@ -724,13 +764,13 @@ def main():
         print(json.dumps(out), flush=True)
         return
 
-    if a.workload in ("mixed", "large", "precision", "coev", "plain"):
+    if a.workload in ("mixed", "large", "precision", "coev", "plain", "f64"):
         if rank != 0:
             return
         import torch
         torch.cuda.set_device(0)
         out = {"mixed": run_mixed, "large": run_large, "precision": run_precision, "coev": run_coev,
-               "plain": run_plain_small}[a.workload](a)
+               "plain": run_plain_small, "f64": run_f64}[a.workload](a)
         out.update({"metric": METRIC if a.workload == "mixed" else "per-layer time and entropy",
                     "n_gpus": 1, "data": "synthetic (seeded Haar gates and measurement uniforms)"})
         print(json.dumps(out), flush=True)
