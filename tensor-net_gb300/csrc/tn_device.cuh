@@ -641,23 +641,31 @@ __device__ void update_stream(cpx<T> *__restrict__ X, int ld, int rows, const in
 // -- resident path (float, ell <= RES_ROWS, W == 32) ---------------------
 // Slots [s0, s0 + W/2) of Ab (Ab[r][s0 + p] = A[rc[s0 + p]][r]) from A, or
 // back to A; eight independent accesses in flight per thread.  No barrier.
+// Each thread moves a pair of adjacent slots (p, p + 1) of one row: two
+// coalesced global accesses (consecutive lanes, consecutive rows) and one
+// 16-byte shared access, which with the even row pitch is free of bank
+// conflicts within each quarter warp.
 template <typename T, int NT, int W>
 __device__ void load_half_res(const cpx<T> *__restrict__ A, int ell, const int *rc, int s0, Smem<T, W> &sm) {
-  constexpr int TP = SmemLayout<T, W>::AP, B = W / 2, UN = 8;
-  const int tot = B * ell;
+  constexpr int TP = SmemLayout<T, W>::AP, B = W / 2, UN = 4;
+  static_assert(TP % 2 == 0 && sizeof(T) == 4, "16-byte pairs");
+  const int tot = (B / 2) * ell;
   for (int base = threadIdx.x; base < tot; base += NT * UN) {
-    cpx<T> v[UN];
+    cpx<T> v0[UN], v1[UN];
 #pragma unroll
     for (int u = 0; u < UN; ++u) {
       const int idx = base + u * NT;
-      const int p = idx / ell, r = idx - p * ell;
-      v[u] = (idx < tot && rc[s0 + p] >= 0) ? A[size_t(rc[s0 + p]) * ell + r] : czero<T>();
+      const int pp = idx / ell, r = idx - pp * ell;
+      const int c0 = idx < tot ? rc[s0 + 2 * pp] : -1, c1 = idx < tot ? rc[s0 + 2 * pp + 1] : -1;
+      v0[u] = c0 >= 0 ? A[size_t(c0) * ell + r] : czero<T>();
+      v1[u] = c1 >= 0 ? A[size_t(c1) * ell + r] : czero<T>();
     }
 #pragma unroll
     for (int u = 0; u < UN; ++u) {
       const int idx = base + u * NT;
-      const int p = idx / ell, r = idx - p * ell;
-      if (idx < tot) sm.Ab[r * TP + s0 + p] = v[u];
+      const int pp = idx / ell, r = idx - pp * ell;
+      if (idx < tot)
+        *reinterpret_cast<float4 *>(sm.Ab + r * TP + s0 + 2 * pp) = make_float4(v0[u].x, v0[u].y, v1[u].x, v1[u].y);
     }
   }
 }
@@ -665,9 +673,13 @@ __device__ void load_half_res(const cpx<T> *__restrict__ A, int ell, const int *
 template <typename T, int NT, int W>
 __device__ void store_half_res(cpx<T> *__restrict__ A, int ell, const int *rc, int s0, const Smem<T, W> &sm) {
   constexpr int TP = SmemLayout<T, W>::AP, B = W / 2;
-  for (int idx = threadIdx.x; idx < B * ell; idx += NT) {
-    const int p = idx / ell, r = idx - p * ell;
-    if (rc[s0 + p] >= 0) A[size_t(rc[s0 + p]) * ell + r] = sm.Ab[r * TP + s0 + p];
+  static_assert(TP % 2 == 0 && sizeof(T) == 4, "16-byte pairs");
+  for (int idx = threadIdx.x; idx < (B / 2) * ell; idx += NT) {
+    const int pp = idx / ell, r = idx - pp * ell;
+    const float4 v = *reinterpret_cast<const float4 *>(sm.Ab + r * TP + s0 + 2 * pp);
+    const int c0 = rc[s0 + 2 * pp], c1 = rc[s0 + 2 * pp + 1];
+    if (c0 >= 0) A[size_t(c0) * ell + r] = mkc<T>(v.x, v.y);
+    if (c1 >= 0) A[size_t(c1) * ell + r] = mkc<T>(v.z, v.w);
   }
 }
 
@@ -739,27 +751,37 @@ __device__ void update_res(int ell, const cpx<T> *__restrict__ Jm, Smem<T, W> &s
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[i][j] = czero<T>();
-  for (int p = 0; p < W; ++p) {
-    cpx<T> jr[8], a[4];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) jr[j] = Jm[p * (W + 1) + q0 + j];
+  static_assert(TP % 2 == 0 && sizeof(T) == 4, "16-byte pairs");
+  for (int p = 0; p < W; p += 2) {
+    // slots p, p + 1 of each of the thread's rows in one 16-byte read
+    float4 a2[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int r = rb + i * RB;
-      a[i] = r < ell ? sm.Ab[r * TP + p] : czero<T>();
+      a2[i] = r < ell ? *reinterpret_cast<const float4 *>(sm.Ab + r * TP + p) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int h = 0; h < 2; ++h) {
+      cpx<T> jr[8];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) acc[i][j] = cfma(a[i], jr[j], acc[i][j]);
+      for (int j = 0; j < 8; ++j) jr[j] = Jm[(p + h) * (W + 1) + q0 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const cpx<T> a = h ? mkc<T>(a2[i].z, a2[i].w) : mkc<T>(a2[i].x, a2[i].y);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = cfma(a, jr[j], acc[i][j]);
+      }
+    }
   }
   __syncthreads();
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const int r = rb + i * RB;
     if (r < ell) {
+      float4 *dst = reinterpret_cast<float4 *>(sm.Ab + r * TP + q0);
 #pragma unroll
-      for (int j = 0; j < 8; ++j) sm.Ab[r * TP + q0 + j] = acc[i][j];
+      for (int j = 0; j < 4; ++j)
+        dst[j] = make_float4(acc[i][2 * j].x, acc[i][2 * j].y, acc[i][2 * j + 1].x, acc[i][2 * j + 1].y);
     }
   }
   __syncthreads();
