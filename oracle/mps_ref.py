@@ -1,9 +1,11 @@
 """FP64 CPU oracle for the Schmidt-form (Gamma-Lambda) MPS trajectory path.
 
 TEST INFRASTRUCTURE ONLY.  Nothing in the product path may import, call or
-execute this module; only ``tests/``, ``__graft_entry__.smoke()`` and the
-``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` use it, and only as
-the checker or the timed CPU baseline.
+execute this module; only ``tests/`` (including the golden-fixture generator),
+``__graft_entry__.smoke()`` and the CPU-baseline legs of ``bench.py``
+(``cpu_baseline``, ``--impl reference``, the single-core timing of
+``--workload plain``) use it, and only as the checker or the timed CPU
+baseline.
 
 This is a step-by-step restatement of whooie/tensor-net's ``MPS<Q, C64>``
 (``tensor-net/lib/mps.rs``), its Haar sampler (``tensor-net/lib/gate.rs``) and
