@@ -683,56 +683,73 @@ __device__ void store_half_res(cpx<T> *__restrict__ A, int ell, const int *rc, i
   }
 }
 
-// G = Ab^H Ab.  Warp w computes rows 8(w % 4) .. +7 of G over the rows
-// r = w / 4 (mod 4) of Ab, lane q holding column q: eight broadcast loads and
-// one row load feed 8 complex FMAs per lane and row.  The four partial sums
-// (G itself, two 32 x 32 tiles in region 0 -- free during the Jacobi steps --
-// and Ts) are then added in a fixed order.
+// G = Ab^H Ab, Hermitian: only the three 16 x 16 tiles G_II, G_IJ and G_JJ
+// (I = slots 0-15, J = slots 16-31) are formed, G_JI = G_IJ^H is filled in
+// after.  Warp w < 15 computes tile w % 3 over the rows r = w / 3 (mod 5) of
+// Ab; lane = (tile column c = lane % 16, row half h = lane / 16), eight rows
+// per lane read as four 16-byte broadcasts per half-warp.  The five partial
+// sums (G itself, two compact tiles' worth in region 0 and one each in Ts and
+// J, all free at this point) are added in a fixed order.
 template <typename T, int NT, int W>
 __device__ void gram_res(int ell, Smem<T, W> &sm) {
   static_assert(W == 32 && NT == 512, "resident Gram assumes W = 32, 16 warps");
-  static_assert(SmemLayout<T, W>::theta_bytes >= 2 * W * W * sizeof(cpx<T>), "partials fit region 0");
-  constexpr int TP = SmemLayout<T, W>::AP, GP = W + 1, RS = 8, KS = 4;
+  constexpr int TP = SmemLayout<T, W>::AP, GP = W + 1, RS = 8, KS = 5, NTILE = 3, TE = 256;
   static_assert(TP % 2 == 0, "16-byte aligned rows");
+  static_assert(SmemLayout<T, W>::theta_bytes >= 2 * NTILE * TE * sizeof(cpx<T>), "two partials fit region 0");
+  static_assert(SmemLayout<T, W>::ts_bytes >= NTILE * TE * sizeof(cpx<T>), "a partial fits Ts");
+  static_assert(SmemLayout<T, W>::g_bytes >= NTILE * TE * sizeof(cpx<T>), "a partial fits J");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int p0 = RS * (warp % KS), ks = warp / KS;
+  const int tile = warp % NTILE, ks = warp / NTILE;  // warp 15: ks = 5, idle
+  const int row0 = tile == 2 ? 16 : 0, col0 = tile == 0 ? 0 : 16;
+  const int c = lane & 15, h = lane >> 4;
+  const int p0 = row0 + 8 * h, q = col0 + c;
   cpx<T> acc[RS];
 #pragma unroll
   for (int i = 0; i < RS; ++i) acc[i] = czero<T>();
-  int r = ks;
-  for (; r + KS < ell; r += 2 * KS) {
-    const cpx<T> *row0 = sm.Ab + r * TP, *row1 = row0 + KS * TP;
-    cpx<T> x0[RS], x1[RS];
-    // eight consecutive complex values of each row as four 16-byte broadcasts
-    const float4 *v0 = reinterpret_cast<const float4 *>(row0 + p0), *v1 = reinterpret_cast<const float4 *>(row1 + p0);
+  if (ks < KS) {
+    int r = ks;
+    for (; r + KS < ell; r += 2 * KS) {
+      const cpx<T> *ra = sm.Ab + r * TP, *rb = ra + KS * TP;
+      const float4 *v0 = reinterpret_cast<const float4 *>(ra + p0), *v1 = reinterpret_cast<const float4 *>(rb + p0);
+      const cpx<T> y0 = ra[q], y1 = rb[q];
 #pragma unroll
-    for (int i = 0; i < RS / 2; ++i) {
-      const float4 a = v0[i], b = v1[i];
-      x0[2 * i] = mkc<T>(a.x, a.y);
-      x0[2 * i + 1] = mkc<T>(a.z, a.w);
-      x1[2 * i] = mkc<T>(b.x, b.y);
-      x1[2 * i + 1] = mkc<T>(b.z, b.w);
+      for (int i = 0; i < RS / 2; ++i) {
+        const float4 a = v0[i], b = v1[i];
+        acc[2 * i] = cjfma(mkc<T>(b.x, b.y), y1, cjfma(mkc<T>(a.x, a.y), y0, acc[2 * i]));
+        acc[2 * i + 1] = cjfma(mkc<T>(b.z, b.w), y1, cjfma(mkc<T>(a.z, a.w), y0, acc[2 * i + 1]));
+      }
     }
-    const cpx<T> y0 = row0[lane], y1 = row1[lane];
+    if (r < ell) {
+      const cpx<T> *ra = sm.Ab + r * TP;
+      const cpx<T> y0 = ra[q];
 #pragma unroll
-    for (int i = 0; i < RS; ++i) acc[i] = cjfma(x1[i], y1, cjfma(x0[i], y0, acc[i]));
+      for (int i = 0; i < RS; ++i) acc[i] = cjfma(ra[p0 + i], y0, acc[i]);
+    }
   }
-  if (r < ell) {
-    const cpx<T> *row0 = sm.Ab + r * TP;
-    const cpx<T> y0 = row0[lane];
-#pragma unroll
-    for (int i = 0; i < RS; ++i) acc[i] = cjfma(row0[p0 + i], y0, acc[i]);
-  }
-  // partials 1, 2 unpadded (pitch W: 2 W^2 values fit region 0), 3 in Ts (pitch W + 1)
+  // partial ks: 0 -> G (pitch GP); 1, 2 -> region 0; 3 -> Ts; 4 -> J (compact, tile-major)
   cpx<T> *r0 = reinterpret_cast<cpx<T> *>(sm.r0);
-  cpx<T> *dst = ks == 0 ? sm.G : (ks == 1 ? r0 : (ks == 2 ? r0 + W * W : sm.Ts));
-  const int pitch = (ks == 1 || ks == 2) ? W : GP;
+  cpx<T> *P1 = r0, *P2 = r0 + NTILE * TE, *P3 = sm.Ts, *P4 = sm.J;
+  if (ks == 0) {
 #pragma unroll
-  for (int i = 0; i < RS; ++i) dst[(p0 + i) * pitch + lane] = acc[i];
+    for (int i = 0; i < RS; ++i) sm.G[(p0 + i) * GP + q] = acc[i];
+  } else if (ks < KS) {
+    cpx<T> *dst = ks == 1 ? P1 : (ks == 2 ? P2 : (ks == 3 ? P3 : P4));
+#pragma unroll
+    for (int i = 0; i < RS; ++i) dst[tile * TE + (8 * h + i) * 16 + c] = acc[i];
+  }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < W * W; idx += NT) {
-    const int o = (idx / W) * GP + idx % W;
-    sm.G[o] = cadd(cadd(sm.G[o], r0[idx]), cadd(r0[W * W + idx], sm.Ts[o]));
+  for (int idx = threadIdx.x; idx < NTILE * TE; idx += NT) {
+    const int t = idx / TE, e = idx % TE, a = e / 16, b = e % 16;
+    const int pp = (t == 2 ? 16 : 0) + a, qq = (t == 0 ? 0 : 16) + b;
+    const int o = pp * GP + qq;
+    sm.G[o] = cadd(cadd(sm.G[o], P1[idx]), cadd(cadd(P2[idx], P3[idx]), P4[idx]));
+  }
+  __syncthreads();
+  // G_JI = G_IJ^H
+  for (int idx = threadIdx.x; idx < TE; idx += NT) {
+    const int a = idx / 16, b = idx % 16;
+    const cpx<T> v = sm.G[b * GP + 16 + a];
+    sm.G[(16 + a) * GP + b] = mkc<T>(v.x, -v.y);
   }
   __syncthreads();
 }
