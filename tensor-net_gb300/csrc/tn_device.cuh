@@ -878,9 +878,9 @@ __device__ const cpx<T> *jacobi_gram(Smem<T, W> &sm, const int *cols, T tol, T t
     // R on (p, q): column p = (c, -s e), column q = (s, c e)
     T c = T(1), sn = T(0);
     cpx<T> e = mkc<T>(T(1), T(0));
-    bool rot = false;
-    if (cols[p] >= 0 && cols[q] >= 0)
-      rot = jacobi_rotation<T>(G[p * GP + p].x, G[q * GP + q].x, G[p * GP + q], tol, tiny2, c, sn, e);
+    // an empty slot (cols < 0) holds a zero vector, so its Gram diagonal is 0
+    // <= tiny2 and jacobi_rotation declines the pair without reading cols
+    const bool rot = jacobi_rotation<T>(G[p * GP + p].x, G[q * GP + q].x, G[p * GP + q], tol, tiny2, c, sn, e);
     __syncwarp();  // every lane has read the pivot entries before row p, q change
     if (rot) {
       // rows: G[p][j] <- c G[p][j] - s conj(e) G[q][j];  G[q][j] <- s G[p][j] + c conj(e) G[q][j]
