@@ -280,8 +280,9 @@ int tn_batch_tuning(tn_batch *b, int32_t *cfg, double *scores);
 int tn_batch_set_schedule(tn_batch *b, int32_t schedule);
 /* Jacobi tuning of the batch (picked by the autotuner): scheme 0 visits all
  * vector pairs of each block pair of a sweep, scheme 1 visits every pair once
- * per sweep (within-block steps, then cross-block steps); max_sweeps bounds
- * the sweeps of one SVD (1..200, default 40). */
+ * per sweep (within-block steps, then cross-block steps), scheme 2 is scheme 0
+ * with two inner sweeps per block step during the first two sweeps;
+ * max_sweeps bounds the sweeps of one SVD (1..200, default 40). */
 int tn_batch_set_tuning(tn_batch *b, int32_t scheme, int32_t max_sweeps);
 /* Device time of the last non-graph step, split into the gate launch (all
  * gates of the layer as independent items) and the sweep launch (measurement

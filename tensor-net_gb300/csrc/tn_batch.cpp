@@ -748,7 +748,7 @@ int tn_batch_set_schedule(tn_batch *b, int32_t schedule) {
 }
 
 int tn_batch_set_tuning(tn_batch *b, int32_t scheme, int32_t max_sweeps) {
-  if (!b || scheme < 0 || scheme > 1 || max_sweeps < 1 || max_sweeps > 200) return TN_ERR_INVALID_ARG;
+  if (!b || scheme < 0 || scheme > 2 || max_sweeps < 1 || max_sweeps > 200) return TN_ERR_INVALID_ARG;
   for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);  // captured launches carry the old values
   b->graphs.clear();
   b->scheme = scheme;

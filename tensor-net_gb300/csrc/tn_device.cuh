@@ -847,7 +847,7 @@ __device__ __forceinline__ bool jacobi_rotation<float>(float a, float b, cpx<flo
 // then, after a barrier, R to columns p, q of G and J (lane = row).  Pairs
 // of one round are disjoint, so each element has one writer per phase.
 template <typename T, int NT, int W>
-__device__ const cpx<T> *jacobi_gram(Smem<T, W> &sm, const int *cols, T tol, T tiny2, int mode) {
+__device__ const cpx<T> *jacobi_gram(Smem<T, W> &sm, const int *cols, T tol, T tiny2, int mode, int inner = 1) {
   constexpr int H = W / 2, GP = W + 1;
   static_assert(W == 32 && NT / 32 == H, "one warp per rotation pair");
   cpx<T> *G = sm.G, *J = sm.J;
@@ -862,7 +862,7 @@ __device__ const cpx<T> *jacobi_gram(Smem<T, W> &sm, const int *cols, T tol, T t
   // across the two halves (H rounds); mode 2: only pairs within each half
   // (H-1 rounds).  Every round rotates H disjoint pairs.
   const int rounds = mode == 0 ? W - 1 : (mode == 1 ? H : H - 1);
-  for (int r = 0; r < rounds; ++r) {
+  for (int r = 0; r < rounds * inner; ++r) {
     int p, q;
     if (mode == 0) {
       rr_pair<W>(r, t, p, q);
@@ -984,7 +984,13 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
     // block pairs (2b, 2b+1) rotating only pairs inside each block, then one
     // step per block pair I < J rotating only pairs across the two blocks.
     // Slots [0, B) hold block I, [B, W) block J; cols[t] = -1 marks an empty slot.
-    const int ndiag = (nblk <= 2 || scheme == 0) ? 0 : (nblk + 1) / 2;
+    // scheme 0: every step rotates all pairs of its block pair; 1: within-block
+    // steps, then cross-block steps; 2: as 0 with two inner sweeps per step in
+    // the first two outer sweeps (fewer outer sweeps for far-from-orthogonal
+    // starts, such as a gate's theta)
+    const int pscheme = scheme == 1 ? 1 : 0;
+    const int inner = (scheme == 2 && sweep < 2) ? 2 : 1;
+    const int ndiag = (nblk <= 2 || pscheme == 0) ? 0 : (nblk + 1) / 2;
     const int nsteps = (nblk <= 2) ? 1 : ndiag + nblk * (nblk - 1) / 2;
     int I = 0, Jb = 1;
     for (int st = 0; st < nsteps; ++st) {
@@ -998,7 +1004,7 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
         bi = 2 * st;
         bj = (2 * st + 1 < nblk) ? 2 * st + 1 : -1;
       } else {
-        mode = scheme == 0 ? 0 : 1;
+        mode = pscheme == 0 ? 0 : 1;
         bi = I;
         bj = Jb;
         if (++Jb >= nblk) {
@@ -1086,7 +1092,7 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
       cyc[3] += 1;
       if (need) {
         rotated = 1;
-        const cpx<T> *Jm = jacobi_gram<T, NT, W>(sm, cols, tol, tiny2, mode);
+        const cpx<T> *Jm = jacobi_gram<T, NT, W>(sm, cols, tol, tiny2, mode, inner);
         long long t2 = clock64();
         cyc[1] += t2 - t1;
         t1 = t2;
