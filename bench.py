@@ -58,7 +58,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--schedule", type=int, default=1, choices=[0, 1])
-    ap.add_argument("--scheme", type=int, default=0, choices=[0, 1, 2], help="Jacobi block-pair scheme")
+    ap.add_argument("--scheme", type=int, default=None, choices=[0, 1, 2, 3],
+                    help="Jacobi block scheme (default: the library's)")
     ap.add_argument("--runs", type=int, default=64, help="coev: sampled trajectories")
     ap.add_argument("--workload", default="batch", choices=["batch", "mixed", "large", "precision", "coev", "plain",
                                                                  "f64"],
@@ -294,7 +295,8 @@ def run_gpu(a, rank, world, local_rank):
     batch = pkg.Batch([n] * B, [trunc] * B, a.prec)
     batch.set_schedule(a.schedule)
     batch.set_theta_path(a.theta == "simt")
-    batch.set_tuning(a.scheme, 40)
+    if a.scheme is not None:
+        batch.set_tuning(a.scheme, 40)
     traj0 = rank * B
     total_layers = a.prefill + a.warmup + 2 * a.steps
 

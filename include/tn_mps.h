@@ -261,8 +261,8 @@ int tn_batch_slot_bytes(tn_batch *b, uint32_t t, uint64_t *bytes);
 int tn_batch_set_theta_path(tn_batch *b, int32_t simt);
 /* Online autotuner: the next 4 * trial_steps host- or pointer-launched steps
  * (tn_batch_step, tn_batch_step_ptrs) run, trial_steps each, the candidate
- * configurations {schedule 1, Jacobi scheme 0, tensor-core theta},
- * {1, 1, tensor-core}, {0, 0, tensor-core}, {1, 0, SIMT theta}; each is
+ * configurations {schedule 1, Jacobi scheme 3, tensor-core theta},
+ * {1, 0, tensor-core}, {0, 3, tensor-core}, {1, 3, SIMT theta}; each is
  * scored by device launch time per algorithmic flop (device counters), and
  * the best is kept (captured graphs are re-captured with it).  trial_steps
  * = 0 stops tuning.  Results are the same under every candidate up to the
@@ -280,9 +280,10 @@ int tn_batch_tuning(tn_batch *b, int32_t *cfg, double *scores);
 int tn_batch_set_schedule(tn_batch *b, int32_t schedule);
 /* Jacobi tuning of the batch (picked by the autotuner): scheme 0 visits all
  * vector pairs of each block pair of a sweep, scheme 1 visits every pair once
- * per sweep (within-block steps, then cross-block steps), scheme 2 is scheme 0
- * with two inner sweeps per block step during the first two sweeps;
- * max_sweeps bounds the sweeps of one SVD (1..200, default 40). */
+ * per sweep (within-block steps, then cross-block steps), scheme 2 / 3 is
+ * scheme 0 with two inner sweeps per block step during the first two / three
+ * sweeps (default 3); max_sweeps bounds the sweeps of one SVD (1..200,
+ * default 40). */
 int tn_batch_set_tuning(tn_batch *b, int32_t scheme, int32_t max_sweeps);
 /* Device time of the last non-graph step, split into the gate launch (all
  * gates of the layer as independent items) and the sweep launch (measurement

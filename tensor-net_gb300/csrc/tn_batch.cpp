@@ -51,7 +51,7 @@ struct tn_batch {
   cudaStream_t st = nullptr;
   int sms = 1, bps = 1, grid_max = 1;
   int maxcap = 1, maxn = 1, sortP = 1, pcap = 8;
-  int scheme = 0, max_sweeps = 40;  // Jacobi tuning (tn_batch_set_tuning)
+  int scheme = kDefaultScheme, max_sweeps = 40;  // Jacobi tuning (tn_batch_set_tuning)
   int theta_simt = 0;               // 1: SIMT theta contraction instead of the tensor-core one
   // Online autotuner (tn_batch_autotune): the next steps run each candidate
   // configuration for `trial` steps; the score of a candidate is launch time
@@ -201,7 +201,7 @@ StepPtrs ptrs_of(const StepLayout &L, char *dbase) {
 
 // Candidate configurations of the autotuner: {schedule, Jacobi scheme, SIMT theta}.
 constexpr int kTuneCands = 4;
-constexpr int kTuneTable[kTuneCands][3] = {{1, 0, 0}, {1, 1, 0}, {0, 0, 0}, {1, 0, 1}};
+constexpr int kTuneTable[kTuneCands][3] = {{1, 3, 0}, {1, 0, 0}, {0, 3, 0}, {1, 3, 1}};
 
 // Algorithmic flops counted so far over every slot (theta + SVD counters).
 int stats_flops(tn_batch *b, double *flops) {
@@ -748,7 +748,7 @@ int tn_batch_set_schedule(tn_batch *b, int32_t schedule) {
 }
 
 int tn_batch_set_tuning(tn_batch *b, int32_t scheme, int32_t max_sweeps) {
-  if (!b || scheme < 0 || scheme > 2 || max_sweeps < 1 || max_sweeps > 200) return TN_ERR_INVALID_ARG;
+  if (!b || scheme < 0 || scheme > 3 || max_sweeps < 1 || max_sweeps > 200) return TN_ERR_INVALID_ARG;
   for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);  // captured launches carry the old values
   b->graphs.clear();
   b->scheme = scheme;

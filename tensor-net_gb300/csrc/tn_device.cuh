@@ -988,8 +988,8 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
     // steps, then cross-block steps; 2: as 0 with two inner sweeps per step in
     // the first two outer sweeps (fewer outer sweeps for far-from-orthogonal
     // starts, such as a gate's theta)
-    const int pscheme = scheme == 1 ? 1 : 0;
-    const int inner = (scheme == 2 && sweep < 2) ? 2 : 1;
+    const int pscheme = scheme == 1 ? 1 : 0;  // scheme 3: as 2 over the first three sweeps
+    const int inner = (scheme == 2 && sweep < 2) || (scheme == 3 && sweep < 3) ? 2 : 1;
     const int ndiag = (nblk <= 2 || pscheme == 0) ? 0 : (nblk + 1) / 2;
     const int nsteps = (nblk <= 2) ? 1 : ndiag + nblk * (nblk - 1) / 2;
     int I = 0, Jb = 1;

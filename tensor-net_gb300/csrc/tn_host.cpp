@@ -305,6 +305,7 @@ int mps_run(tn_mps *m, const std::vector<Instr> &prog, const std::vector<double>
     la.ws = L.ws.p;
     la.ws_stride = run_work_bytes(m->prec, L.ws_cap);
     la.max_sweeps = kMaxSweeps;
+    la.jacobi_scheme = kDefaultScheme;
     CK(launch_run(m->prec, la, grid, L.sortP, L.ws_cap, m->st));
     if (prog.empty()) return TN_OK;
   }
@@ -341,6 +342,7 @@ int mps_run(tn_mps *m, const std::vector<Instr> &prog, const std::vector<double>
   la.ws = L.ws.p;
   la.ws_stride = 0;
   la.max_sweeps = kMaxSweeps;
+  la.jacobi_scheme = kDefaultScheme;
   CK(launch_run(m->prec, la, 1, L.sortP, L.ws_cap, m->st));
   bool sync = false;
   if (outc && n_meas_out > 0) {

@@ -107,6 +107,10 @@ struct LaunchArgs {
   int *qerr;              // set to 1 when a queue wait ran past its time limit
 };
 
+// Default Jacobi block scheme (see jacobi_svd): all pairs of each block pair,
+// two inner sweeps per step during the first three sweeps.
+constexpr int kDefaultScheme = 3;
+
 // Wait limit of a CTA on a pushed queue slot (nanoseconds of %globaltimer).
 constexpr unsigned long long kQueueWaitNs = 120ull * 1000 * 1000 * 1000;
 

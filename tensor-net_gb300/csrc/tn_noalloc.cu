@@ -123,6 +123,7 @@ extern "C" int tn_mps_apply_unitary2_noalloc(tn_mps *m, uint32_t k, const double
   la.ws = s->scratch;
   la.ws_stride = 0;
   la.max_sweeps = 40;
+  la.jacobi_scheme = tn::kDefaultScheme;
   e = tn::launch_run(v.prec, la, 1, tn::next_pow2(2 * v.cap), v.cap, v.st);
   if (e != cudaSuccess) {
     tn::set_last_error("tn_mps_apply_unitary2_noalloc: launch", e);

@@ -328,6 +328,6 @@ def test_autotuner_tries_every_candidate_and_keeps_the_best(pkg):
     assert not st["tuning"]
     assert all(s > 0 for s in st["scores"])
     best = int(np.argmin(st["scores"]))
-    cand = [(1, 0, 0), (1, 1, 0), (0, 0, 0), (1, 0, 1)][best]
+    cand = [(1, 3, 0), (1, 0, 0), (0, 3, 0), (1, 3, 1)][best]
     assert (st["schedule"], st["scheme"], st["theta_simt"]) == cand
     assert tuned.device_status() == 0
