@@ -116,6 +116,64 @@ class MPS:
                 "apply_unitary2")
         return self
 
+    def apply_gate(self, gate, rng=None):
+        """``apply_gate`` / ``apply_gate_rng`` (mps.rs:2044-2069): the gate's
+        matrix through ``apply_unitary1`` or ``apply_unitary2``; out-of-range
+        qubits are a no-op.  ``rng`` feeds ``Haar2``."""
+        k, m = gate.into_matrix(rng)
+        if gate.is_q1():
+            return self.apply_unitary1(k, m)
+        return self.apply_unitary2(k, m)
+
+    def apply_circuit(self, gates, rng=None):
+        """``apply_circuit`` / ``apply_circuit_rng`` (mps.rs:2071-2088)."""
+        for g in gates:
+            self.apply_gate(g, rng)
+        return self
+
+    def apply_uni(self, uni, rng=None):
+        """``apply_uni`` / ``apply_uni_rng`` (mps.rs:2093-2126): a ``Mat`` must
+        be 2x2 or 4x4, otherwise ``TN_ERR_OPERATOR_SHAPE``."""
+        if uni.is_gate():
+            return self.apply_gate(uni.gate, rng)
+        shape = np.shape(uni.matrix)
+        if shape == (2, 2):
+            return self.apply_unitary1(uni.k, uni.matrix)
+        # 4x4 and every other shape: the C ABI answers TN_ERR_OPERATOR_SHAPE for the latter
+        return self.apply_unitary2(uni.k, uni.matrix)
+
+    def apply_meas_prob(self, meas, u: float = 0.0):
+        """``apply_meas_prob`` (mps.rs:2138-2150): ``Rand`` samples with the
+        uniform ``u``, ``Proj`` post-selects; ``None`` when out of range."""
+        if meas.is_rand():
+            return self.measure_prob(meas.k, u)
+        pr = self.measure_postsel_prob(meas.k, meas.outcome)
+        return None if pr is None else (meas.outcome, pr)
+
+    def apply_meas(self, meas, u: float = 0.0):
+        """``apply_meas`` (mps.rs:2131-2135)."""
+        r = self.apply_meas_prob(meas, u)
+        return None if r is None else r[0]
+
+    def apply_meas_layer_ops(self, meas, us=None):
+        """``apply_meas_prob_layer`` over ``Meas`` values (mps.rs:2206-2252):
+        targets are filtered, de-duplicated (first kept) and sorted as there;
+        ``us[j]`` is the uniform of the j-th surviving target in ascending
+        qubit order (ignored for a ``Proj``)."""
+        meas = list(meas)
+        ks = [m.k for m in meas]
+        posts = [-1 if m.is_rand() else m.outcome for m in meas]
+        return self.apply_meas_prob_layer(ks, us if us is not None else np.zeros(len(meas)), posts)
+
+    def apply_bilayer_ops(self, unis, meas, us=None, rng=None):
+        """``circuit::apply_bilayer`` (circuit.rs:624-659) over ``Uni`` and
+        ``Meas`` sequences: returns (outcomes as ``Meas.proj``, [(k, prob)])."""
+        from .gates import Meas
+        for u in unis:
+            self.apply_uni(u, rng)
+        res = self.apply_meas_layer_ops(meas, us)
+        return [Meas.proj(k, o) for (k, o, _) in res], [(k, p) for (k, _, p) in res]
+
     # ---- probabilities / measurement
     def probs(self, k: int):
         """``probs`` (mps.rs:1071-1076)."""
