@@ -32,10 +32,36 @@ def run_uniforms(seed: int, run: int, layer: int, count: int) -> np.ndarray:
 
 
 def run_coevolution(n: int, depth: int, p: float, runs: int, seed: int, circuit: int = 0,
-                    bonds=REFERENCE_BONDS, precision: str = "f64", cutoff: float = 1e-12):
-    """Returns dict(outcomes[runs, M], probs[runs, len(bonds), M], sites[M, 2]
-    (layer, qubit)) with M the circuit's number of measurements; the last
-    entry of `bonds` must be None (the sampled trajectories)."""
+                    bonds=REFERENCE_BONDS, precision: str = "f64"):
+    """Coevolution of the seeded brickwork circuit ``gen_layer(seed, circuit,
+    t, n, p)``, t < depth.  Returns dict(outcomes[runs, M], probs[runs,
+    len(bonds), M], sites[M, 2] (layer, qubit)) with M the circuit's number of
+    measurements; the last entry of `bonds` must be None (the sampled
+    trajectories)."""
+    layers = [gen_layer(seed, circuit, t, n, p)[:3] for t in range(depth)]
+    return run_coevolution_layers(n, layers, runs, seed, bonds, precision)
+
+
+def run_coevolution_files(manifest_path, circ: int, p: float, runs: int, seed: int,
+                          bonds=REFERENCE_BONDS, precision: str = "f64"):
+    """The reference driver's inputs (haar_coev_probs.rs:96-140): a
+    ``MiptManifest`` CBOR file, a circuit number and a p of the manifest; the
+    unitary and measurement CBOR files are read from the manifest's folder."""
+    import os
+
+    from .circuits import MiptManifest, batch_layer
+    man = MiptManifest.load(manifest_path)
+    unis, meas = man.load_circuit(os.path.dirname(os.path.abspath(manifest_path)), circ, p)
+    if len(unis) != len(meas):
+        raise ValueError("unitary and measurement files differ in depth")
+    layers = [batch_layer(u, m) for u, m in zip(unis, meas)]
+    return run_coevolution_layers(man.nqubits, layers, runs, seed, bonds, precision)
+
+
+def run_coevolution_layers(n: int, layers, runs: int, seed: int, bonds=REFERENCE_BONDS,
+                           precision: str = "f64"):
+    """Coevolution over explicit layers ``[(gate_ks, gates[ng, 4, 4], meas_ks)]``;
+    run r draws its outcome uniforms from ``run_uniforms(seed, r, t, .)``."""
     assert bonds[-1] is None, "the untruncated sampler comes last"
     chis = [c for c in bonds if c is not None]
     sampler = Batch([n] * runs, [Trunc.none()] * runs, precision)
@@ -43,10 +69,12 @@ def run_coevolution(n: int, depth: int, p: float, runs: int, seed: int, circuit:
     s_ids = list(range(runs))
     r_ids = list(range(runs * len(chis)))
     outcomes, probs, sites = [], [], []
-    for t in range(depth):
-        gk, g, mk, _ = gen_layer(seed, circuit, t, n, p)
-        layers = [(gk, g, mk, run_uniforms(seed, r, t, len(mk))) for r in range(runs)]
-        recs, _ = sampler.step(s_ids, layers)
+    for t, (gk, g, mk) in enumerate(layers):
+        # the surviving targets in the order the layer measures them (mps.rs:2214-2220),
+        # so that outcome j of the sampler is post-selection j of the replays
+        mk = np.unique(np.asarray(mk, np.int64)[np.asarray(mk, np.int64) < n]).astype(np.uint32)
+        slayers = [(gk, g, mk, run_uniforms(seed, r, t, len(mk))) for r in range(runs)]
+        recs, _ = sampler.step(s_ids, slayers)
         post = [np.array([o for (_, o, _) in recs[r]], np.int32) for r in range(runs)]
         rlayers = [(gk, g, mk, np.zeros(len(mk))) for r in range(runs) for _ in chis]
         rposts = [post[r] for r in range(runs) for _ in chis]
