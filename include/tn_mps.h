@@ -98,6 +98,17 @@ int tn_device_info(char *name, uint32_t cap, uint32_t *sm_count);
 int tn_mps_new_qubits(uint32_t n, const tn_trunc *trunc, int32_t precision,
                       uint32_t chi_cap, tn_mps **out);
 int tn_mps_free(tn_mps *m);
+/* MPS::from_vector over qubits (mps.rs:517-550, factorize mps.rs:448-505):
+ * state = 2^n interleaved complex128 amplitudes (s_0 most significant), len =
+ * number of amplitudes.  Normalised, then factorised left to right on the
+ * device (float64 one-sided Jacobi SVD per site, process_svd's rank rule with
+ * `trunc`, NULL = Cutoff(f64::EPSILON)).  chi_cap 0 picks chi_max for
+ * CONST/BOTH, else 2^(n/2).  n == 0 -> TN_ERR_EMPTY_SYSTEM; len != 2^n ->
+ * TN_ERR_STATE_SHAPE; n > 20, a NULL state or a zero / non-finite norm ->
+ * TN_ERR_INVALID_ARG. */
+int tn_mps_from_vector(uint32_t n, const double *state, uint64_t len,
+                       const tn_trunc *trunc, int32_t precision,
+                       uint32_t chi_cap, tn_mps **out);
 /* #[derive(Clone)] (mps.rs:338). */
 int tn_mps_clone(const tn_mps *m, tn_mps **out);
 int tn_mps_n(const tn_mps *m, uint32_t *n);

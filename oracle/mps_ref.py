@@ -402,6 +402,41 @@ class MPS:
         return max((len(s) for s in self.svals), default=None)
 
 
+def from_vector(state, trunc: Trunc | None = None) -> MPS:
+    """``MPS::from_vector`` over qubits (mps.rs:517-550) with ``factorize``
+    (mps.rs:448-505): normalise, then left to right reshape the remainder to
+    (2 chi_{k-1}, rest), SVD + ``process_svd``, Gamma_k = U[:, :rank] reshaped
+    (chi_{k-1}, 2, rank) divided by Lambda_{k-1} on its first axis, carry q on;
+    the last Gamma is q reshaped (chi_{n-2}, 2, 1) divided by Lambda_{n-2}."""
+    psi = np.asarray(state, dtype=np.complex128).reshape(-1)
+    n = int(round(math.log2(psi.size))) if psi.size else 0
+    if psi.size == 0:
+        raise ValueError("EmptySystem")
+    if (1 << n) != psi.size:
+        raise ValueError("StateIncompatibleShape")
+    psi = psi / math.sqrt(float(np.sum(np.abs(psi) ** 2)))
+    m = MPS(n, trunc)
+    if n == 1:
+        m.data[0] = psi.reshape(1, 2, 1).copy()
+        return m
+    tr = trunc if trunc is not None else Trunc.none()
+    q = psi.reshape(1, -1)
+    udim = 1
+    for k in range(n - 1):
+        q = q.reshape(udim * 2, -1)
+        u, s, q, rank = local_decomp(q, tr)
+        g = u.reshape(udim, 2, rank).copy()
+        if k > 0:
+            g /= m.svals[k - 1][:, None, None]
+        m.data[k] = g
+        m.svals[k] = s
+        udim = rank
+    g = q.reshape(udim, 2, 1).copy()
+    g /= m.svals[n - 2][:, None, None]
+    m.data[n - 1] = g
+    return m
+
+
 def apply_bilayer(mps: MPS, gate_ks, gates, meas_ks, us):
     """``circuit::apply_bilayer`` (circuit.rs:624-659) with ``Uni::Mat`` gates
     (``apply_uni_rng`` -> ``apply_unitary2``, mps.rs:2110-2126) followed by one

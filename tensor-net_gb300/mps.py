@@ -76,6 +76,20 @@ class MPS:
         """``MPS::new_qubits`` (mps.rs:2033-2039)."""
         return cls(n, trunc, precision, chi_cap)
 
+    @classmethod
+    def from_vector(cls, state, trunc: Trunc | None = None, precision: str = "f64", chi_cap: int = 0):
+        """``MPS::from_vector`` over qubits (mps.rs:517-550): normalise the
+        2^n amplitudes (s_0 most significant) and factorise them on the GPU
+        (``tn_mps_from_vector``); n <= 20."""
+        a = np.ascontiguousarray(np.asarray(state, dtype=np.complex128).reshape(-1))
+        n = max(int(a.size).bit_length() - 1, 0)
+        buf = a.view(np.float64).reshape(-1) if a.size else np.zeros(1)
+        tr = C.byref(trunc.c()) if trunc is not None else None
+        h = C.c_void_p()
+        L.check(L.lib().tn_mps_from_vector(n if a.size else 0, L.dptr(buf), a.size, tr, PRECISIONS[precision],
+                                           int(chi_cap), C.byref(h)), "tn_mps_from_vector")
+        return cls(0, _handle=h)
+
     def close(self):
         if self._h:
             self._lib.tn_mps_free(self._h)

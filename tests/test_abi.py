@@ -57,6 +57,21 @@ def test_empty_system_is_an_error(pkg):
     assert lib.tn_mps_new_qubits(0, None, 0, 0, ctypes.byref(h)) == -1
 
 
+def test_from_vector_argument_errors(pkg):
+    """from_vector's MPSError cases (mps.rs:517-530) come before any device work."""
+    lib = pkg.lib()
+    h = ctypes.c_void_p()
+    psi = np.zeros(2 * 8)
+    p = psi.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    assert lib.tn_mps_from_vector(0, p, 0, None, 0, 0, ctypes.byref(h)) == -1   # EmptySystem
+    assert lib.tn_mps_from_vector(3, p, 6, None, 0, 0, ctypes.byref(h)) == -4   # StateIncompatibleShape
+    assert lib.tn_mps_from_vector(21, p, 1 << 21, None, 0, 0, ctypes.byref(h)) == -6
+    assert lib.tn_mps_from_vector(3, None, 8, None, 0, 0, ctypes.byref(h)) == -6
+    with pytest.raises(pkg.TnError) as e:
+        pkg.MPS.from_vector(np.ones(6))
+    assert e.value.status == -4
+
+
 def test_haar_matches_independent_qr(pkg, ref):
     """tn_haar_u4 (MGS QR) equals gate::haar's Householder QR + phase fix."""
     for site in range(6):

@@ -55,3 +55,19 @@ def test_coevolution_replay_matches_oracle(pkg, ref):
                 np.testing.assert_allclose(out["probs"][r, ci, col:col + len(mk)], [q for (_, _, q) in rr],
                                            atol=1e-9)
             col += len(mk)
+
+
+def test_coevolution_from_cbor_circuit_files(pkg, tmp_path):
+    """The reference driver's inputs (a MiptManifest and its CBOR unitary /
+    measurement files) give the same coevolution as the same circuit fed as
+    arrays."""
+    from tensor_net_gb300 import circuits
+    from tensor_net_gb300.coev import run_coevolution, run_coevolution_files
+    man = circuits.MiptManifest.new(5, 8, 6, 1, [0.2])
+    man.save_all(tmp_path)
+    a = run_coevolution_files(tmp_path / man.manifest_fname(), 0, 0.2, 2, 9, bonds=(4, 8, None))
+    b = run_coevolution(8, 6, 0.2, 2, 9, circuit=0, bonds=(4, 8, None))
+    np.testing.assert_array_equal(a["sites"], b["sites"])
+    np.testing.assert_array_equal(a["outcomes"], b["outcomes"])
+    np.testing.assert_array_equal(a["probs"], b["probs"])
+    assert a["device_status"] == (0, 0)

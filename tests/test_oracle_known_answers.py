@@ -218,3 +218,24 @@ def test_last_site_measurement_leaves_last_bond_stale():
     proj = dense_project(psi, n, n - 1, 0)
     assert abs(abs(np.vdot(m.contract(), proj)) - 1.0) < 1e-12
     assert abs(m.entropy_vn(n - 2) - LN2) < 1e-12  # the true entropy is 0
+
+
+def test_oracle_from_vector_factorize():
+    """factorize (mps.rs:448-505): the contraction gives back the normalised
+    vector; the bond-0 Schmidt values are those of the dense reshape; GHZ and
+    product states have ranks 2 and 1."""
+    rng = np.random.default_rng(2)
+    n = 7
+    psi = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+    m = R.from_vector(psi)
+    np.testing.assert_allclose(m.contract(), psi / np.linalg.norm(psi), atol=1e-13)
+    for b in range(n - 1):
+        s = np.linalg.svd((psi / np.linalg.norm(psi)).reshape(1 << (b + 1), -1), compute_uv=False)
+        np.testing.assert_allclose(m.svals[b], s[: len(m.svals[b])], atol=1e-13)
+    t = R.from_vector(psi, R.Trunc.const(3))
+    assert [len(s) for s in t.svals] == [2, 3, 3, 3, 3, 2]
+    ghz = np.zeros(1 << n)
+    ghz[0] = ghz[-1] = 1
+    assert [len(s) for s in R.from_vector(ghz).svals] == [2] * (n - 1)
+    one = R.from_vector(np.array([0.6, 0.8j]))
+    assert one.n == 1 and np.allclose(one.data[0].reshape(-1), [0.6, 0.8j])
