@@ -38,6 +38,7 @@ extern "C" {
 enum {
     TN_OK = 0,
     TN_NONE = 1,                     /* reference returns None (out-of-range query) */
+    TN_CANCELLED = 2,                /* tn_result.status of a request ended by tn_server_cancel */
     TN_ERR_EMPTY_SYSTEM = -1,        /* MPSError::EmptySystem            mps.rs:131 */
     TN_ERR_INVALID_QNUM = -2,        /* MPSError::InvalidQuantumNumber   mps.rs:136 */
     TN_ERR_UNPHYSICAL_INDEX = -3,    /* MPSError::UnphysicalIndex        mps.rs:141 */
@@ -359,6 +360,13 @@ int tn_server_submit(tn_server *s, const tn_request *r, double arrival, uint64_t
 int tn_server_tick(tn_server *s, uint32_t *n_active, uint32_t *n_done);
 /* Completed requests (up to cap). */
 int tn_server_poll(tn_server *s, tn_result *out, uint32_t cap, uint32_t *n);
+/* Cancel request `id`.  A queued request is dropped at once; a resident one
+ * is retired when the layer it is part of finishes (no kernel of the server
+ * is using its memory after that), its slot and arena range freed.  Either
+ * way a tn_result with status TN_CANCELLED and the layers completed so far
+ * is queued for tn_server_poll.  TN_NONE if the id is unknown or already
+ * finished. */
+int tn_server_cancel(tn_server *s, uint64_t id);
 /* [0] traj-layers run, [1] seconds inside ticks, [2] ticks, [3] arena bytes in
  * use, [4] pending, [5] active, [6] admitted, [7] completed. */
 int tn_server_stats(const tn_server *s, double *out);

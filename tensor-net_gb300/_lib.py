@@ -14,9 +14,9 @@ u32, i32, u64, dbl = C.c_uint32, C.c_int32, C.c_uint64, C.c_double
 P = C.POINTER
 vp = C.c_void_p
 
-TN_OK, TN_NONE = 0, 1
+TN_OK, TN_NONE, TN_CANCELLED = 0, 1, 2
 STATUS = {
-    0: "TN_OK", 1: "TN_NONE", -1: "TN_ERR_EMPTY_SYSTEM", -2: "TN_ERR_INVALID_QNUM",
+    0: "TN_OK", 1: "TN_NONE", 2: "TN_CANCELLED", -1: "TN_ERR_EMPTY_SYSTEM", -2: "TN_ERR_INVALID_QNUM",
     -3: "TN_ERR_UNPHYSICAL_INDEX", -4: "TN_ERR_STATE_SHAPE", -5: "TN_ERR_OPERATOR_SHAPE",
     -6: "TN_ERR_INVALID_ARG", -7: "TN_ERR_CUDA", -8: "TN_ERR_OOM", -9: "TN_ERR_CAPACITY",
     -10: "TN_ERR_NOT_CONVERGED", -11: "TN_ERR_PROB_SUM", -12: "TN_ERR_NO_DEVICE",
@@ -100,6 +100,7 @@ SIGNATURES = {
     "tn_server_submit": (C.c_int, [vp, P(tn_request), dbl, P(u64)]),
     "tn_server_tick": (C.c_int, [vp, P(u32), P(u32)]),
     "tn_server_poll": (C.c_int, [vp, P(tn_result), u32, P(u32)]),
+    "tn_server_cancel": (C.c_int, [vp, u64]),
     "tn_server_stats": (C.c_int, [vp, P(dbl)]),
     "tn_haar_u4": (C.c_int, [P(dbl), P(dbl)]),
     "tn_gen_layer": (C.c_int, [u64, u64, u32, u32, dbl, P(u32), P(dbl), P(u32), P(u32), P(dbl), P(u32)]),

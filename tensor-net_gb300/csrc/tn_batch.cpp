@@ -519,6 +519,11 @@ int tn_batch_step_post(tn_batch *b, const uint32_t *trajs, uint32_t nt, const ui
       if (j > meas_off[i] && meas_ks[j] <= meas_ks[j - 1]) return TN_ERR_INVALID_ARG;
     }
   }
+  // non-finite gate entries or uniforms are refused before any device work
+  for (size_t j = 0; j < size_t(ng) * 32; ++j)
+    if (!std::isfinite(gates[j])) return TN_ERR_INVALID_ARG;
+  for (uint32_t j = 0; j < nm; ++j)
+    if (!std::isfinite(us[j])) return TN_ERR_INVALID_ARG;
   int need = 8;
   for (uint32_t i = 0; i < nt; ++i)
     need = std::max<int>(need, int(gate_off[i + 1] - gate_off[i]) + int(meas_off[i + 1] - meas_off[i]) +

@@ -188,6 +188,7 @@ const char *tn_status_string(int s) {
   switch (s) {
     case TN_OK: return "ok";
     case TN_NONE: return "none (out of range)";
+    case TN_CANCELLED: return "cancelled";
     case TN_ERR_EMPTY_SYSTEM: return "error in MPS creation: cannot create for an empty system";
     case TN_ERR_INVALID_QNUM: return "error in MPS creation: invalid quantum number";
     case TN_ERR_UNPHYSICAL_INDEX: return "error in MPS creation: unphysical zero-dimensional physical index";
@@ -400,6 +401,14 @@ int read_lam(const tn_mps *m, uint32_t b, int len, std::vector<double> &out) {
 
 bool gate_shape_ok(uint32_t rows, uint32_t cols, uint32_t d) { return rows == d && cols == d; }
 
+// A non-finite gate entry would spread NaN / inf through the bond's Schmidt
+// values and every later operation; it is refused before any device work.
+bool all_finite(const double *x, size_t n) {
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(x[i])) return false;
+  return true;
+}
+
 }  // namespace
 
 extern "C" {
@@ -518,6 +527,7 @@ int tn_mps_apply_unitary1(tn_mps *m, uint32_t k, const double *op, uint32_t rows
   if (!m || !op) return TN_ERR_INVALID_ARG;
   if (k >= m->n) return TN_OK;
   if (!gate_shape_ok(rows, cols, 2)) return TN_ERR_OPERATOR_SHAPE;
+  if (!all_finite(op, 8)) return TN_ERR_INVALID_ARG;
   std::vector<double> g(32, 0.0);
   std::memcpy(g.data(), op, 8 * sizeof(double));
   return mps_run(m, {Instr{OP_UNI1, int(k), 0, 0}}, g, {}, 0, nullptr, nullptr, 0, nullptr, 0, nullptr);
@@ -527,6 +537,7 @@ int tn_mps_apply_unitary2(tn_mps *m, uint32_t k, const double *op, uint32_t rows
   if (!m || !op) return TN_ERR_INVALID_ARG;
   if (m->n == 1 || k >= m->n - 1) return TN_OK;
   if (!gate_shape_ok(rows, cols, 4)) return TN_ERR_OPERATOR_SHAPE;
+  if (!all_finite(op, 32)) return TN_ERR_INVALID_ARG;
   std::vector<double> g(op, op + 32);
   return mps_run(m, {Instr{OP_GATE, int(k), 0, 0}}, g, {}, 0, nullptr, nullptr, 0, nullptr, 0, nullptr);
 }
@@ -550,6 +561,7 @@ int tn_mps_prob(const tn_mps *m, uint32_t k, uint32_t p, double *out) {
 int tn_mps_measure_prob(tn_mps *m, uint32_t k, double u, int32_t *outcome, double *prob) {
   if (!m) return TN_ERR_INVALID_ARG;
   if (k >= m->n) return TN_NONE;
+  if (!std::isfinite(u)) return TN_ERR_INVALID_ARG;
   std::vector<Instr> prog{Instr{OP_MEAS, int(k), 0, -1}};
   emit_sweep(prog, m->n);
   int32_t oc = 0;
@@ -611,6 +623,7 @@ int tn_mps_apply_meas_prob_layer(tn_mps *m, const uint32_t *ks, uint32_t nk, con
   std::vector<double> u(tk.size(), 0.0);
   if (us)
     for (size_t j = 0; j < tk.size(); ++j) u[j] = us[j];
+  if (!all_finite(u.data(), u.size())) return TN_ERR_INVALID_ARG;
   std::vector<Instr> prog;
   emit_meas_layer(prog, m->n, tk, tp, 0);
   std::vector<int32_t> oc(tk.size());
@@ -629,6 +642,7 @@ int tn_mps_apply_bilayer(tn_mps *m, const uint32_t *gate_ks, const double *gates
                          const uint32_t *meas_ks, uint32_t nm, const double *us, uint32_t *out_ks,
                          int32_t *outcomes, double *probs, uint32_t *n_out) {
   if (!m || (ng && (!gate_ks || !gates)) || (nm && (!meas_ks || !us))) return TN_ERR_INVALID_ARG;
+  if (ng && !all_finite(gates, size_t(ng) * 32)) return TN_ERR_INVALID_ARG;
   std::vector<Instr> prog, par;
   std::vector<double> g;
   g.reserve(size_t(ng) * 32);
@@ -648,6 +662,7 @@ int tn_mps_apply_bilayer(tn_mps *m, const uint32_t *gate_ks, const double *gates
   std::vector<int32_t> tp;
   select_targets(m->n, meas_ks, nm, nullptr, tk, tp);
   std::vector<double> u(us, us + tk.size());
+  if (!all_finite(u.data(), u.size())) return TN_ERR_INVALID_ARG;
   emit_meas_layer(prog, m->n, tk, tp, 0);
   if (n_out) *n_out = uint32_t(tk.size());
   std::vector<int32_t> oc(std::max<size_t>(1, tk.size()));

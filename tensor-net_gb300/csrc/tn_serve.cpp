@@ -103,6 +103,7 @@ struct Active {
   uint32_t layer = 0;
   size_t off = 0, bytes = 0;
   double entropy = 0;
+  bool cancel = false;  // retire when the layer in flight finishes
 };
 
 // One cost class: an engine (slots bound to arena memory), its queue, and
@@ -211,6 +212,7 @@ int admit(tn_server *s, Class &c) {
     a.off = off;
     a.bytes = bytes;
     a.entropy = 0;
+    a.cancel = false;
     s->admitted += 1;
     c.active += 1;
     c.pending.erase(c.pending.begin() + std::ptrdiff_t(pi));
@@ -264,7 +266,26 @@ int launch(tn_server *s, Class &c) {
   return TN_OK;
 }
 
-// Reads the entropies of the finished layer and retires completed requests.
+// Frees a resident request's slot and arena range and queues its result.
+void retire(tn_server *s, Class &c, uint32_t slot, int32_t status, double t_end) {
+  Active &a = c.act[slot];
+  tn_result res{};
+  res.id = a.id;
+  res.layers = a.layer;
+  res.final_entropy = a.entropy;
+  res.latency_s = t_end - a.t_arrival;
+  res.queue_s = a.t_admit - a.t_arrival;
+  res.status = status;
+  s->done.push_back(res);
+  s->alloc.release(a.off, a.bytes);
+  a.on = false;
+  a.cancel = false;
+  c.active -= 1;
+  c.free_slots.push_back(slot);
+}
+
+// Reads the entropies of the finished layer and retires completed (and
+// cancelled) requests.
 int collect(tn_server *s, Class &c, uint32_t *ndone) {
   const uint32_t nt = uint32_t(c.trajs.size());
   c.ents.resize(std::max<uint32_t>(nt, 1));
@@ -276,19 +297,11 @@ int collect(tn_server *s, Class &c, uint32_t *ndone) {
     a.entropy = c.ents[j];
     a.layer += 1;
     if (a.layer >= a.r.depth) {
-      tn_result res{};
-      res.id = a.id;
-      res.layers = a.layer;
-      res.final_entropy = a.entropy;
-      res.latency_s = t_end - a.t_arrival;
-      res.queue_s = a.t_admit - a.t_arrival;
-      res.status = 0;
-      s->done.push_back(res);
-      s->alloc.release(a.off, a.bytes);
-      a.on = false;
-      c.active -= 1;
-      c.free_slots.push_back(c.trajs[j]);
+      retire(s, c, c.trajs[j], TN_OK, t_end);
       s->completed += 1;
+      ++*ndone;
+    } else if (a.cancel) {
+      retire(s, c, c.trajs[j], TN_CANCELLED, t_end);
       ++*ndone;
     }
   }
@@ -449,6 +462,35 @@ int tn_server_stats(const tn_server *s, double *out) {
   out[6] = s->admitted;
   out[7] = s->completed;
   return TN_OK;
+}
+
+int tn_server_cancel(tn_server *s, uint64_t id) {
+  if (!s) return TN_ERR_INVALID_ARG;
+  for (int i = 0; i < s->ncls; ++i) {
+    Class &c = s->cls[i];
+    for (size_t j = 0; j < c.pending.size(); ++j) {
+      if (c.pending[j].id != id) continue;
+      tn_result res{};
+      res.id = id;
+      res.latency_s = s->now() - c.pending[j].t_arrival;
+      res.queue_s = res.latency_s;
+      res.status = TN_CANCELLED;
+      s->done.push_back(res);
+      c.pending.erase(c.pending.begin() + std::ptrdiff_t(j));
+      return TN_OK;
+    }
+    for (uint32_t slot = 0; slot < uint32_t(c.act.size()); ++slot) {
+      Active &a = c.act[slot];
+      if (!a.on || a.id != id) continue;
+      if (c.inflight) {
+        a.cancel = true;  // its layer is running: retired by collect()
+      } else {
+        retire(s, c, slot, TN_CANCELLED, s->now());
+      }
+      return TN_OK;
+    }
+  }
+  return TN_NONE;
 }
 
 int tn_server_set_policy(tn_server *s, int32_t policy, uint32_t max_active0, uint32_t max_active1) {

@@ -61,6 +61,13 @@ class Server:
         return [dict(id=r.id, layers=r.layers, final_entropy=r.final_entropy, latency_s=r.latency_s,
                      queue_s=r.queue_s, status=r.status) for r in buf[: n.value]]
 
+    def cancel(self, req_id: int) -> bool:
+        """Cancel a queued or resident request (``tn_server_cancel``); its
+        result (status ``TN_CANCELLED``) appears in ``poll``.  False when the
+        id is unknown or already finished."""
+        s = L.check(self._lib.tn_server_cancel(self._h, int(req_id)), "tn_server_cancel")
+        return s == L.TN_OK
+
     def stats(self):
         out = np.zeros(8)
         L.check(self._lib.tn_server_stats(self._h, L.dptr(out)), "tn_server_stats")

@@ -111,3 +111,42 @@ def test_least_work_policy_and_active_cap(pkg):
         out[policy] = (order, res[big]["final_entropy"], res[small]["final_entropy"])
     assert out["fcfs"][0][0] == 1 and out["least-work"][0][0] == 2
     assert out["fcfs"][1:] == out["least-work"][1:]
+
+
+def test_cancel_queued_and_resident_requests(pkg):
+    """A queued request is dropped at once; a resident one is retired when its
+    layer in flight finishes, freeing its memory for the next request; the
+    other requests' results are untouched (failure handling on the host, no
+    GPU fault involved)."""
+    n, chi = 12, 32
+    per = n * chi * chi * 2 * 8 + 8 * chi * (n + 1) + 4 * (n + 1)
+    s = pkg.Server(int(per * 1.5) + 4096, max_slots=4, precision="mixed", max_chi=32, max_n=16)
+    tr = pkg.Trunc.both(chi, 1e-10)
+    a = s.submit(n, tr, 0.1, 8, 5, 0)   # resident first
+    b = s.submit(n, tr, 0.1, 4, 5, 1)   # waits for memory
+    c = s.submit(n, tr, 0.1, 4, 5, 2)   # waits, then cancelled while queued
+    assert s.cancel(c)
+    got = {d["id"]: d for d in s.poll()}
+    assert got[c]["status"] == pkg.STATUS_CANCELLED and got[c]["layers"] == 0
+    s.tick()
+    s.tick()
+    assert s.stats()["active"] == 1 and s.stats()["pending"] == 1
+    assert s.cancel(a)                  # resident: retired after its current layer
+    done = {}
+    for _ in range(30):
+        s.tick()
+        done.update({d["id"]: d for d in s.poll()})
+        if b in done:
+            break
+    assert done[a]["status"] == pkg.STATUS_CANCELLED and 0 < done[a]["layers"] < 8
+    assert done[b]["status"] == 0 and done[b]["layers"] == 4
+    assert not s.cancel(a) and not s.cancel(12345)
+    assert s.stats()["arena_used"] == 0
+    # b's result equals the same request run alone
+    s2 = pkg.Server(1 << 30, max_slots=4, precision="mixed", max_chi=32, max_n=16)
+    i = s2.submit(n, tr, 0.1, 4, 5, 1)
+    res = []
+    while not res:
+        s2.tick()
+        res = s2.poll()
+    assert res[0]["id"] == i and res[0]["final_entropy"] == done[b]["final_entropy"]
