@@ -26,6 +26,10 @@ thread_local std::string g_last_error;
 
 void tn::set_last_error(const char *what, cudaError_t e) {
   g_last_error = e == cudaSuccess ? std::string(what) : std::string(what) + ": " + cudaGetErrorString(e);
+  // A failed call also becomes the runtime's "last error" of this thread; a
+  // non-sticky one (a refused allocation) would otherwise be reported again
+  // by the cudaGetLastError() after the next kernel launch.  Consume it.
+  if (e != cudaSuccess) (void)cudaGetLastError();
 }
 
 namespace {
