@@ -110,9 +110,25 @@ int tn_mps_free(tn_mps *m);
 int tn_mps_from_vector(uint32_t n, const double *state, uint64_t len,
                        const tn_trunc *trunc, int32_t precision,
                        uint32_t chi_cap, tn_mps **out);
+/* Checkpoint / resume: a state from its parts in the reference layout, the
+ * inverse of tn_mps_export_gamma + tn_mps_svals (the reference has no
+ * serialisation of MPS, mps.rs:338).  chi[n + 1] are the bond dimensions
+ * with chi[0] = chi[n] = 1; gammas = Gamma_0 .. Gamma_{n-1} concatenated, each
+ * (chi[k], 2, chi[k + 1]) row-major interleaved complex128; lams =
+ * Lambda_0 .. Lambda_{n-2} concatenated (chi[1] .. chi[n-1] values).  The
+ * parts are taken as they are (a state exported from a handle resumes
+ * bit for bit in the same precision).  chi_cap 0 picks the larger of the
+ * widest bond and the tn_mps_new_qubits rule.  chi[0] or chi[n] != 1 or a
+ * zero bond -> TN_ERR_STATE_SHAPE; a bond above chi_cap -> TN_ERR_CAPACITY;
+ * non-finite entries -> TN_ERR_INVALID_ARG. */
+int tn_mps_import(uint32_t n, const uint32_t *chi, const double *gammas,
+                  const double *lams, const tn_trunc *trunc, int32_t precision,
+                  uint32_t chi_cap, tn_mps **out);
 /* #[derive(Clone)] (mps.rs:338). */
 int tn_mps_clone(const tn_mps *m, tn_mps **out);
 int tn_mps_n(const tn_mps *m, uint32_t *n);
+/* The handle's tn_precision. */
+int tn_mps_precision(const tn_mps *m, int32_t *precision);
 /* get_trunc / set_trunc (mps.rs:1216-1221); set_trunc(NULL) = None. */
 int tn_mps_get_trunc(const tn_mps *m, tn_trunc *out);
 int tn_mps_set_trunc(tn_mps *m, const tn_trunc *trunc);

@@ -47,9 +47,11 @@ SIGNATURES = {
     "tn_mps_free": (C.c_int, [vp]),
     "tn_mps_clone": (C.c_int, [vp, P(vp)]),
     "tn_mps_n": (C.c_int, [vp, P(u32)]),
+    "tn_mps_precision": (C.c_int, [vp, P(i32)]),
     "tn_mps_get_trunc": (C.c_int, [vp, P(tn_trunc)]),
     "tn_mps_set_trunc": (C.c_int, [vp, P(tn_trunc)]),
     "tn_mps_from_vector": (C.c_int, [u32, P(dbl), u64, P(tn_trunc), i32, u32, P(vp)]),
+    "tn_mps_import": (C.c_int, [u32, P(u32), P(dbl), P(dbl), P(tn_trunc), i32, u32, P(vp)]),
     "tn_mps_apply_unitary1": (C.c_int, [vp, u32, P(dbl), u32, u32]),
     "tn_mps_apply_unitary2": (C.c_int, [vp, u32, P(dbl), u32, u32]),
     "tn_mps_apply_unitary2_noalloc": (C.c_int, [vp, u32, P(dbl), u32, u32]),

@@ -503,9 +503,73 @@ int tn_mps_clone(const tn_mps *src, tn_mps **out) {
   return TN_OK;
 }
 
+// Checkpoint / resume: a state from its reference-layout parts (the inverse
+// of tn_mps_export_gamma + tn_mps_svals).
+int tn_mps_import(uint32_t n, const uint32_t *chi, const double *gammas, const double *lams, const tn_trunc *trunc,
+                  int32_t precision, uint32_t chi_cap, tn_mps **out) {
+  if (!out) return TN_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (n == 0) return TN_ERR_EMPTY_SYSTEM;
+  if (!chi || !gammas || (n > 1 && !lams)) return TN_ERR_INVALID_ARG;
+  if (chi[0] != 1 || chi[n] != 1) return TN_ERR_STATE_SHAPE;
+  uint32_t widest = 1;
+  size_t ng = 0, nl = 0;
+  for (uint32_t k = 0; k < n; ++k) {
+    if (chi[k + 1] == 0) return TN_ERR_STATE_SHAPE;
+    widest = std::max(widest, chi[k + 1]);
+    ng += size_t(chi[k]) * 2 * chi[k + 1];
+    if (k + 1 < n) nl += chi[k + 1];
+  }
+  if (!all_finite(gammas, 2 * ng) || (nl && !all_finite(lams, nl))) return TN_ERR_INVALID_ARG;
+  uint32_t cap = chi_cap;
+  if (!cap) cap = std::max(default_cap(n, trunc), widest);
+  if (widest > cap || widest > max_schmidt_rank(n)) return TN_ERR_CAPACITY;
+  tn_mps *m = nullptr;
+  if (int s = tn_mps_new_qubits(n, trunc, precision, cap, &m)) return s;
+  if (m->cap < widest) {
+    tn_mps_free(m);
+    return TN_ERR_CAPACITY;
+  }
+  const size_t slot = size_t(2) * m->cap * m->cap * elem_bytes(m->prec);
+  std::vector<int> ichi(chi, chi + n + 1);
+  std::vector<float> tmp;
+  cudaError_t e = cudaStreamSynchronize(m->st);
+  size_t go = 0, lo = 0;
+  for (uint32_t k = 0; k < n && e == cudaSuccess; ++k) {
+    const size_t cnt = size_t(chi[k]) * 2 * chi[k + 1];  // complex entries of Gamma_k
+    char *dst = static_cast<char *>(m->gamma.p) + slot * k;
+    if (m->prec == TN_PREC_F64) {
+      e = cudaMemcpy(dst, gammas + 2 * go, cnt * 16, cudaMemcpyHostToDevice);
+    } else {
+      tmp.resize(2 * cnt);
+      for (size_t i = 0; i < 2 * cnt; ++i) tmp[i] = float(gammas[2 * go + i]);
+      e = cudaMemcpy(dst, tmp.data(), cnt * 8, cudaMemcpyHostToDevice);
+    }
+    go += cnt;
+    if (e == cudaSuccess && k + 1 < n) {
+      e = cudaMemcpy(m->lam.as<double>() + size_t(k + 1) * m->cap, lams + lo, sizeof(double) * chi[k + 1],
+                     cudaMemcpyHostToDevice);
+      lo += chi[k + 1];
+    }
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(m->chi.p, ichi.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    tn_mps_free(m);
+    return cuda_fail(e, "import");
+  }
+  *out = m;
+  return TN_OK;
+}
+
 int tn_mps_n(const tn_mps *m, uint32_t *n) {
   if (!m || !n) return TN_ERR_INVALID_ARG;
   *n = m->n;
+  return TN_OK;
+}
+
+int tn_mps_precision(const tn_mps *m, int32_t *precision) {
+  if (!m || !precision) return TN_ERR_INVALID_ARG;
+  *precision = m->prec;
   return TN_OK;
 }
 

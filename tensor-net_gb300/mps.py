@@ -90,6 +90,53 @@ class MPS:
                                            int(chi_cap), C.byref(h)), "tn_mps_from_vector")
         return cls(0, _handle=h)
 
+    @classmethod
+    def from_parts(cls, gammas, lams, trunc: Trunc | None = None, precision: str = "f64", chi_cap: int = 0):
+        """Checkpoint / resume (``tn_mps_import``): a state from its Gamma
+        tensors (chi_{k-1}, 2, chi_k) and Lambda vectors in the reference
+        layout, as ``export_parts`` returns them."""
+        gs = [np.ascontiguousarray(np.asarray(g, dtype=np.complex128)) for g in gammas]
+        n = len(gs)
+        chi = np.array([1] + [g.shape[2] for g in gs], np.uint32)
+        flat = np.concatenate([g.reshape(-1) for g in gs]).view(np.float64) if n else np.zeros(1)
+        lam = np.concatenate([np.asarray(x, np.float64).reshape(-1) for x in lams]) if len(lams) else np.zeros(1)
+        tr = C.byref(trunc.c()) if trunc is not None else None
+        h = C.c_void_p()
+        L.check(L.lib().tn_mps_import(n, L.uptr(chi), L.dptr(np.ascontiguousarray(flat)),
+                                      L.dptr(np.ascontiguousarray(lam)), tr, PRECISIONS[precision], int(chi_cap),
+                                      C.byref(h)), "tn_mps_import")
+        return cls(0, _handle=h)
+
+    def export_parts(self):
+        """(gammas, lams): every Gamma (chi_{k-1}, 2, chi_k) and Lambda in the
+        reference layout (mps.rs:344-353)."""
+        return [self.gamma(k) for k in range(self.n)], [self.svals(b) for b in range(self.n - 1)]
+
+    def save(self, path):
+        """Write the state, its truncation rule and precision to an npz file."""
+        gs, ls = self.export_parts()
+        t = self.get_trunc()
+        arrays = {f"gamma_{k}": g for k, g in enumerate(gs)}
+        arrays.update({f"lambda_{b}": x for b, x in enumerate(ls)})
+        np.savez(path, n=self.n, precision=self.precision_name(),
+                 trunc=np.array([-1 if t is None else t.mode, 0 if t is None else t.chi_max]),
+                 cutoff=0.0 if t is None else t.cutoff, **arrays)
+
+    @classmethod
+    def load(cls, path, chi_cap: int = 0):
+        """Resume a state written by ``save``."""
+        z = np.load(path)
+        n = int(z["n"])
+        mode, chi_max = (int(x) for x in z["trunc"])
+        trunc = None if mode < 0 else Trunc(mode, chi_max, float(z["cutoff"]))
+        return cls.from_parts([z[f"gamma_{k}"] for k in range(n)], [z[f"lambda_{b}"] for b in range(n - 1)],
+                              trunc, str(z["precision"]), chi_cap)
+
+    def precision_name(self) -> str:
+        p = L.i32()
+        L.check(self._lib.tn_mps_precision(self._h, C.byref(p)), "tn_mps_precision")
+        return {v: k for k, v in PRECISIONS.items()}[int(p.value)]
+
     def close(self):
         if self._h:
             self._lib.tn_mps_free(self._h)

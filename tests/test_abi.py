@@ -57,6 +57,30 @@ def test_empty_system_is_an_error(pkg):
     assert lib.tn_mps_new_qubits(0, None, 0, 0, ctypes.byref(h)) == -1
 
 
+def test_import_argument_errors(pkg):
+    """tn_mps_import's shape checks come before any device work."""
+    lib = pkg.lib()
+    h = ctypes.c_void_p()
+    U = ctypes.POINTER(ctypes.c_uint32)
+    D = ctypes.POINTER(ctypes.c_double)
+    g = np.zeros(64)
+    lam = np.ones(4)
+    for chi, want in (([1, 2, 1], None), ([2, 2, 1], -4), ([1, 0, 1], -4), ([1, 2, 2], -4)):
+        c = np.array(chi, np.uint32)
+        r = lib.tn_mps_import(2, c.ctypes.data_as(U), g.ctypes.data_as(D), lam.ctypes.data_as(D), None, 0, 0,
+                              ctypes.byref(h))
+        if want is not None:
+            assert r == want, (chi, r)
+    assert lib.tn_mps_import(0, None, None, None, None, 0, 0, ctypes.byref(h)) == -1
+    c = np.array([1, 2, 1], np.uint32)
+    bad = g.copy()
+    bad[3] = np.nan
+    assert lib.tn_mps_import(2, c.ctypes.data_as(U), bad.ctypes.data_as(D), lam.ctypes.data_as(D), None, 0, 0,
+                             ctypes.byref(h)) == -6
+    assert lib.tn_mps_import(2, c.ctypes.data_as(U), g.ctypes.data_as(D), lam.ctypes.data_as(D), None, 0, 1,
+                             ctypes.byref(h)) == -9  # a bond of 2 above chi_cap 1
+
+
 def test_from_vector_argument_errors(pkg):
     """from_vector's MPSError cases (mps.rs:517-530) come before any device work."""
     lib = pkg.lib()
