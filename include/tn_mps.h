@@ -228,6 +228,16 @@ int tn_batch_free(tn_batch *b);
 /* Re-initialise slot t to |0...0> with a new n/trunc (n and chi must fit the
  * slot's allocation); used by the serving loop to reuse slots. */
 int tn_batch_reset(tn_batch *b, uint32_t t, uint32_t n, const tn_trunc *trunc);
+/* Slot t := a state given by its reference-layout parts (as tn_mps_import:
+ * chi[n + 1], Gamma_0 .. Gamma_{n-1} and Lambda_0 .. Lambda_{n-2}
+ * concatenated), with truncation rule `trunc`: a prepared initial state
+ * (tn_mps_from_vector) or a checkpoint enters the batch.  n up to the slot's
+ * allocated n, every bond up to the slot's bond capacity (TN_ERR_CAPACITY). */
+int tn_batch_import(tn_batch *b, uint32_t t, uint32_t n, const uint32_t *chi,
+                    const double *gammas, const double *lams, const tn_trunc *trunc);
+/* Gamma of site k of slot t in the reference layout (as tn_mps_export_gamma). */
+int tn_batch_export_gamma(tn_batch *b, uint32_t t, uint32_t k, double *out,
+                          uint64_t cap, uint32_t dims[3]);
 
 /* One brickwork layer for the trajectories listed in `trajs[nt]`:
  * trajectory trajs[i] applies gates gate_off[i]..gate_off[i+1]-1 (sites

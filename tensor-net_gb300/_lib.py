@@ -73,6 +73,8 @@ SIGNATURES = {
     "tn_batch_create": (C.c_int, [u32, P(u32), P(tn_trunc), i32, P(u32), P(vp)]),
     "tn_batch_free": (C.c_int, [vp]),
     "tn_batch_reset": (C.c_int, [vp, u32, u32, P(tn_trunc)]),
+    "tn_batch_import": (C.c_int, [vp, u32, u32, P(u32), P(dbl), P(dbl), P(tn_trunc)]),
+    "tn_batch_export_gamma": (C.c_int, [vp, u32, u32, P(dbl), u64, P(u32)]),
     "tn_batch_step": (C.c_int, [vp, P(u32), u32, P(u32), P(u32), P(dbl), P(u32), P(u32), P(dbl),
                                 P(i32), P(dbl), P(dbl)]),
     "tn_batch_step_post": (C.c_int, [vp, P(u32), u32, P(u32), P(u32), P(dbl), P(u32), P(u32), P(dbl),

@@ -40,6 +40,35 @@ class Batch:
         L.check(self._lib.tn_batch_reset(self._h, int(t), int(n), tr), "tn_batch_reset")
         self.ns[t] = n
 
+    def import_state(self, t: int, gammas, lams, trunc: Trunc | None):
+        """Slot t := the state given by its Gamma / Lambda parts in the
+        reference layout (``tn_batch_import``), e.g. ``MPS.export_parts()``."""
+        gs = [np.ascontiguousarray(np.asarray(g, dtype=np.complex128)) for g in gammas]
+        n = len(gs)
+        chi = np.array([1] + [g.shape[2] for g in gs], np.uint32)
+        flat = np.ascontiguousarray(np.concatenate([g.reshape(-1) for g in gs]).view(np.float64))
+        lam = np.ascontiguousarray(np.concatenate([np.asarray(x, np.float64).reshape(-1) for x in lams])
+                                   if len(lams) else np.zeros(1))
+        tr = C.byref(trunc.c()) if trunc is not None else None
+        L.check(self._lib.tn_batch_import(self._h, int(t), n, L.uptr(chi), L.dptr(flat), L.dptr(lam), tr),
+                "tn_batch_import")
+        self.ns[t] = n
+
+    def gamma(self, t: int, k: int):
+        dims = (L.u32 * 3)()
+        s = L.check(self._lib.tn_batch_export_gamma(self._h, int(t), int(k), None, 0, dims), "export_gamma")
+        if s == L.TN_NONE:
+            return None
+        shape = (dims[0], dims[1], dims[2])
+        out = np.zeros(2 * shape[0] * shape[1] * shape[2])
+        L.check(self._lib.tn_batch_export_gamma(self._h, int(t), int(k), L.dptr(out), out.size, dims),
+                "export_gamma")
+        return out.view(np.complex128).reshape(shape)
+
+    def export_parts(self, t: int):
+        n = int(self.ns[t])
+        return [self.gamma(t, k) for k in range(n)], [self.svals(t, b) for b in range(n - 1)]
+
     @staticmethod
     def pack(trajs, layers):
         """layers[i] = (gate_ks, gates[ng,4,4] complex, meas_ks sorted, us)."""

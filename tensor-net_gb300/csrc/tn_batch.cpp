@@ -495,6 +495,93 @@ int tn_batch_reset(tn_batch *b, uint32_t t, uint32_t n, const tn_trunc *trunc) {
   return TN_OK;
 }
 
+int tn_batch_import(tn_batch *b, uint32_t t, uint32_t n, const uint32_t *chi, const double *gammas, const double *lams,
+                    const tn_trunc *trunc) {
+  if (!b || t >= b->ntraj || (n && (!chi || !gammas || (n > 1 && !lams)))) return TN_ERR_INVALID_ARG;
+  if (n == 0) return TN_ERR_EMPTY_SYSTEM;
+  if (n > b->n_alloc[t]) return TN_ERR_CAPACITY;
+  if (trunc && (trunc->mode < TN_TRUNC_NONE || trunc->mode > TN_TRUNC_BOTH)) return TN_ERR_INVALID_ARG;
+  if (chi[0] != 1 || chi[n] != 1) return TN_ERR_STATE_SHAPE;
+  size_t ng = 0, nl = 0;
+  for (uint32_t k = 0; k < n; ++k) {
+    if (chi[k + 1] == 0) return TN_ERR_STATE_SHAPE;
+    if (chi[k + 1] > b->cap[t]) return TN_ERR_CAPACITY;
+    ng += size_t(chi[k]) * 2 * chi[k + 1];
+    if (k + 1 < n) nl += chi[k + 1];
+  }
+  for (size_t i = 0; i < 2 * ng; ++i)
+    if (!std::isfinite(gammas[i])) return TN_ERR_INVALID_ARG;
+  for (size_t i = 0; i < nl; ++i)
+    if (!std::isfinite(lams[i])) return TN_ERR_INVALID_ARG;
+  // an earlier asynchronous step may still be running on this batch
+  CKB(cudaStreamSynchronize(b->st));
+  TrajDev &d = b->h[t];
+  d.n = int(n);
+  if (trunc) {
+    d.trunc_mode = trunc->mode;
+    d.chi_max = int(std::min<uint32_t>(trunc->chi_max, 0x7fffffff));
+    d.cutoff = trunc->cutoff;
+  } else {
+    d.trunc_mode = TN_TRUNC_NONE;
+    d.chi_max = 0;
+    d.cutoff = 0.0;
+  }
+  const size_t eb = b->prec == TN_PREC_F64 ? 16 : 8;
+  const size_t slot = size_t(2) * d.cap * d.cap * eb;
+  std::vector<float> tmp;
+  size_t go = 0, lo = 0;
+  for (uint32_t k = 0; k < n; ++k) {
+    const size_t cnt = size_t(chi[k]) * 2 * chi[k + 1];
+    char *dst = static_cast<char *>(d.gamma) + slot * k;
+    if (b->prec == TN_PREC_F64) {
+      CKB(cudaMemcpy(dst, gammas + 2 * go, cnt * 16, cudaMemcpyHostToDevice));
+    } else {
+      tmp.resize(2 * cnt);
+      for (size_t i = 0; i < 2 * cnt; ++i) tmp[i] = float(gammas[2 * go + i]);
+      CKB(cudaMemcpy(dst, tmp.data(), cnt * 8, cudaMemcpyHostToDevice));
+    }
+    go += cnt;
+    if (k + 1 < n) {
+      CKB(cudaMemcpy(d.lam + size_t(k + 1) * d.cap, lams + lo, sizeof(double) * chi[k + 1], cudaMemcpyHostToDevice));
+      lo += chi[k + 1];
+    }
+  }
+  const double one = 1.0;
+  CKB(cudaMemcpy(d.lam, &one, sizeof(double), cudaMemcpyHostToDevice));
+  CKB(cudaMemcpy(d.lam + size_t(n) * d.cap, &one, sizeof(double), cudaMemcpyHostToDevice));
+  std::vector<int> ichi(chi, chi + n + 1);
+  CKB(cudaMemcpy(d.chi, ichi.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
+  CKB(cudaMemcpy(b->dtraj + t, &d, sizeof(TrajDev), cudaMemcpyHostToDevice));
+  return TN_OK;
+}
+
+int tn_batch_export_gamma(tn_batch *b, uint32_t t, uint32_t k, double *out, uint64_t cap, uint32_t dims[3]) {
+  if (!b || t >= b->ntraj) return TN_ERR_INVALID_ARG;
+  const TrajDev &d = b->h[t];
+  if (k >= uint32_t(d.n)) return TN_NONE;
+  CKB(cudaStreamSynchronize(b->st));
+  int c[2] = {0, 0};
+  CKB(cudaMemcpy(c, d.chi + k, sizeof(int) * 2, cudaMemcpyDeviceToHost));
+  if (dims) {
+    dims[0] = uint32_t(c[0]);
+    dims[1] = 2;
+    dims[2] = uint32_t(c[1]);
+  }
+  if (!out) return TN_OK;
+  const size_t cnt = size_t(c[0]) * 2 * c[1];
+  if (cap < 2 * cnt) return TN_ERR_INVALID_ARG;
+  const size_t eb = b->prec == TN_PREC_F64 ? 16 : 8;
+  const char *src = static_cast<const char *>(d.gamma) + size_t(2) * d.cap * d.cap * eb * k;
+  if (b->prec == TN_PREC_F64) {
+    CKB(cudaMemcpy(out, src, cnt * 16, cudaMemcpyDeviceToHost));
+  } else {
+    std::vector<float> tmp(2 * cnt);
+    CKB(cudaMemcpy(tmp.data(), src, cnt * 8, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < 2 * cnt; ++i) out[i] = tmp[i];
+  }
+  return TN_OK;
+}
+
 int tn_batch_step(tn_batch *b, const uint32_t *trajs, uint32_t nt, const uint32_t *gate_off, const uint32_t *gate_ks,
                   const double *gates, const uint32_t *meas_off, const uint32_t *meas_ks, const double *us,
                   int32_t *outcomes, double *probs, double *entropy) {

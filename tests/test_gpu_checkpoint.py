@@ -46,3 +46,38 @@ def test_state_from_the_oracle_continues_like_the_oracle(pkg, ref):
     for b in range(n - 1):
         assert abs(g.entropy_vn(b) - r.entropy_vn(b)) < 1e-10
     assert g.device_status() == 0
+
+
+@pytest.mark.parametrize("prec", ["f64", "mixed"])
+def test_prepared_state_enters_a_batch(pkg, prec):
+    """A state factorised from a dense vector (tn_mps_from_vector) enters a
+    batch slot (tn_batch_import) and evolves there exactly as on its own
+    handle; exported back from the batch it continues identically."""
+    n = 10
+    rng = np.random.default_rng(8)
+    psi = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+    tr = pkg.Trunc.both(16, 1e-12)
+    m = pkg.MPS.from_vector(psi, tr, prec)
+    b = pkg.Batch([n, n], [tr, tr], prec)
+    b.import_state(1, *m.export_parts(), tr)
+    for k in range(n):
+        np.testing.assert_array_equal(b.gamma(1, k), m.gamma(k))
+    tol = 1e-10 if prec == "f64" else 1e-5
+    traj = pkg.gen_trajectory(23, 0, n, 8, 0.2)
+
+    def same(r1, r2):
+        assert [x[:2] for x in r1] == [x[:2] for x in r2]
+        for x, y in zip(r1, r2):
+            assert abs(x[2] - y[2]) < tol
+
+    for layer in traj[:4]:
+        recs, ents = b.step([1], [layer])
+        same(recs[0], m.apply_bilayer(*layer))
+        assert abs(ents[0] - m.entropy_vn(n // 2 - 1)) < tol
+    m2 = pkg.MPS.from_parts(*b.export_parts(1), tr, prec)
+    for layer in traj[4:]:
+        same(m2.apply_bilayer(*layer), m.apply_bilayer(*layer))
+    with pytest.raises(pkg.TnError) as e:
+        b.import_state(0, *pkg.MPS.from_vector(psi, None, prec).export_parts(), None)  # bond 32 > capacity 16
+    assert e.value.status == -9
+    assert b.device_status() == 0
