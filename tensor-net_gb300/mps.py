@@ -268,6 +268,77 @@ class MPS:
     def measure_postsel(self, k: int, p: int):
         self.measure_postsel_prob(k, p)
 
+    def measure_reset(self, k: int, u: float):
+        """``measure_reset`` (mps.rs:2278-2286): measure, then apply the
+        reference's ``XMAT`` on outcome 1.  ``XMAT`` is the identity there
+        (gate.rs:649-658), so the site is left in the measured state, as in
+        the reference."""
+        from .gates import make_x
+        r = self.measure(k, u)
+        if r == 1:
+            self.apply_unitary1(k, make_x())
+        return r
+
+    def measure_postsel_reset(self, k: int, p: int):
+        """``measure_postsel_reset`` (mps.rs:2291-2297), with the same ``XMAT``."""
+        from .gates import make_x
+        self.measure_postsel(k, p)
+        if p != 0:
+            self.apply_unitary1(k, make_x())
+
+    def measure_layer(self, ks, us):
+        """``measure_layer`` (mps.rs:1519-1548): outcomes of the surviving
+        targets (filtered, de-duplicated, ascending); ``us[j]`` is the
+        uniform of the j-th of them."""
+        return [o for (_, o, _) in self.apply_meas_prob_layer(ks, us)]
+
+    def measure_prob_layer(self, ks, us):
+        """``measure_prob_layer`` (mps.rs:1552-1582): [(outcome, prob)]."""
+        return [(o, p) for (_, o, p) in self.apply_meas_prob_layer(ks, us)]
+
+    def measure_postsel_prob_layer(self, particles):
+        """``measure_postsel_prob_layer`` (mps.rs:1623-1657): ``particles`` =
+        [(k, p)]; entries with k >= n or p >= 2 are dropped before the
+        de-duplication (first kept), as there; returns the probabilities."""
+        keep = [(int(k), int(p)) for (k, p) in particles if 0 <= int(k) < self.n and int(p) in (0, 1)]
+        if not keep:
+            return []
+        res = self.apply_meas_prob_layer([k for k, _ in keep], np.zeros(len(keep)), [p for _, p in keep])
+        return [pr for (_, _, pr) in res]
+
+    def measure_postsel_layer(self, particles):
+        """``measure_postsel_layer`` (mps.rs:1591-1618)."""
+        self.measure_postsel_prob_layer(particles)
+
+    def apply_unitary2_multi(self, k: int, ops):
+        """``apply_unitary2_multi`` (mps.rs:1393-1414): the product
+        ops[-1] ... ops[0] (4x4 operator constants, multiplied on the host)
+        through one ``apply_unitary2``; a no-op for an out-of-range k, and
+        ``TN_ERR_OPERATOR_SHAPE`` (nothing applied) if any operator is not 4x4."""
+        if self.n == 1 or int(k) >= self.n - 1:
+            return self
+        acc = np.eye(4, dtype=np.complex128)
+        for op in ops:
+            op = np.asarray(op, dtype=np.complex128)
+            if op.shape != (4, 4):
+                raise L.TnError(-5, "apply_unitary2_multi")
+            acc = op @ acc
+        return self.apply_unitary2(k, acc)
+
+    def apply_op_prob(self, op, u: float = 0.0, rng=None):
+        """``apply_op_prob`` (mps.rs:2266-2275): a ``Uni`` is applied (None
+        returned), a ``Meas`` measured ((outcome, prob) or None)."""
+        from .gates import Meas
+        if isinstance(op, Meas):
+            return self.apply_meas_prob(op, u)
+        self.apply_uni(op, rng)
+        return None
+
+    def apply_op(self, op, u: float = 0.0, rng=None):
+        """``apply_op`` (mps.rs:2256-2262)."""
+        r = self.apply_op_prob(op, u, rng)
+        return None if r is None else r[0]
+
     def apply_meas_prob_layer(self, ks, us=None, posts=None):
         """``apply_meas_prob_layer`` (mps.rs:2206-2252): list of (k, outcome, prob)."""
         ks = np.ascontiguousarray(np.asarray(ks, dtype=np.uint32).reshape(-1))
@@ -328,6 +399,18 @@ class MPS:
         out = L.u32()
         s = L.check(self._lib.tn_mps_max_bond_dim(self._h, C.byref(out)), "max_bond_dim")
         return None if s == L.TN_NONE else int(out.value)
+
+    def max_bond_dim_idx(self):
+        """``max_bond_dim_idx`` (mps.rs:1235-1239): Rust's ``max_by_key`` keeps
+        the last of equal maxima."""
+        if self.n < 2:
+            return None
+        dims = [self.bond_dim(b) for b in range(self.n - 1)]
+        best = 0
+        for b, d in enumerate(dims):
+            if d >= dims[best]:
+                best = b
+        return best
 
     def svals(self, b: int):
         ln = L.u32()

@@ -100,3 +100,47 @@ def test_bilayer_ops_with_rand_and_proj_matches_oracle(pkg, ref):
     for b in range(n - 1):
         assert abs(m.entropy_vn(b) - r.entropy_vn(b)) < 1e-10
     assert m.device_status() == 0
+
+
+def test_layer_variants_multi_and_reset_match_the_oracle(pkg, ref):
+    """measure_layer / measure_prob_layer / measure_postsel_(prob_)layer
+    (mps.rs:1519-1657), apply_unitary2_multi (1393-1414), max_bond_dim_idx
+    (1235-1239) and measure_reset (2278-2286) against the oracle."""
+    from tensor_net_gb300 import gates as g
+    n = 8
+    m = pkg.MPS.new_qubits(n, None, "f64")
+    r = ref.MPS(n, None)
+    layers = pkg.gen_trajectory(31, 0, n, 4, 0.0)
+    for (gk, gs, _, _) in layers:
+        for k, u in zip(gk, gs):
+            m.apply_unitary2(int(k), u)
+            r.apply_unitary2(int(k), u)
+    # measure_layer over unsorted duplicates and an out-of-range target
+    ks, us = [5, 2, 9, 5], [0.3, 0.8]
+    out = m.measure_prob_layer(ks, us)
+    want = r.apply_meas_prob_layer(ks, us)
+    assert [o for o, _ in out] == [o for (_, o, _) in want]
+    for (_, p), (_, _, p2) in zip(out, want):
+        assert abs(p - p2) < 1e-10
+    # post-selected layer: (k, p) pairs, invalid p and k dropped before the de-duplication
+    probs = m.measure_postsel_prob_layer([(6, 2), (6, 1), (1, 0), (12, 0)])
+    want = r.apply_meas_prob_layer([1, 6], None, posts=[0, 1])  # the oracle's posts follow the sorted targets
+    assert len(probs) == 2 and all(abs(a - b[2]) < 1e-10 for a, b in zip(probs, want))
+    # apply_unitary2_multi = one apply_unitary2 of the product
+    ops = [pkg.haar_u4(pkg.ginibre(3, 0, 0, j)) for j in range(3)]
+    m.apply_unitary2_multi(3, ops)
+    r.apply_unitary2(3, ops[2] @ ops[1] @ ops[0])
+    for b in range(n - 1):
+        assert abs(m.entropy_vn(b) - r.entropy_vn(b)) < 1e-10
+    with pytest.raises(pkg.TnError):
+        m.apply_unitary2_multi(3, [np.eye(4), np.eye(2)])
+    m.apply_unitary2_multi(7, [np.eye(3)])  # out of range: no-op before the shape check
+    dims = [m.bond_dim(b) for b in range(n - 1)]
+    assert m.max_bond_dim_idx() == max(i for i, d in enumerate(dims) if d == max(dims))
+    # measure_reset: the reference's XMAT is the identity, so outcome 1 stays 1
+    o = m.measure_reset(4, 0.999999)
+    if o == 1:
+        np.testing.assert_allclose(m.probs(4), [0.0, 1.0], atol=1e-12)
+    assert m.apply_op(g.Meas.proj(4, o)) == o
+    assert m.apply_op(g.Uni.of_gate(g.Gate.H(0))) is None
+    assert m.device_status() == 0
