@@ -813,7 +813,9 @@ def main():
         "data": "synthetic (seeded Haar gates and measurement uniforms)",
         "config": dict(config, batch_per_gpu=r["B"], gpu=r["gpu"]),
         "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
-        "gpu_launches": 3 * a.steps,
+        # per timed step: k_lpt_order, k_gate_slots, k_compile_dd, k_run (schedule 1; the launch list in
+        # profiles/), or k_lpt_order, k_compile and two k_run (schedule 0)
+        "gpu_launches": 4 * a.steps,
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "peak_kind": f"{peaks_kind} bf16 sustained",
                      "traffic": (tr["bytes_per_flop"] * per_launch) if tr else None,
