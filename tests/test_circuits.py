@@ -178,3 +178,34 @@ def test_npz_meas_round_trip(pkg, tmp_path):
     ps, groups = circuits.load_meas(f)
     np.testing.assert_array_equal(ps, [0.1, 0.2])
     assert groups == [layers for (_, layers) in meas]
+
+
+def test_cbor_fuzz_round_trip(pkg):
+    """Random nested values survive dumps/loads (hypothesis, CPU only)."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+    from tensor_net_gb300 import _cbor
+    leaves = st.one_of(st.none(), st.booleans(), st.integers(min_value=-(2 ** 64), max_value=2 ** 64 - 1),
+                       st.floats(allow_nan=False), st.text(max_size=40), st.binary(max_size=40))
+    values = st.recursive(leaves, lambda ch: st.one_of(st.lists(ch, max_size=6),
+                                                       st.dictionaries(st.text(max_size=8), ch, max_size=6)),
+                          max_leaves=30)
+
+    @hyp.settings(max_examples=300, deadline=None)
+    @hyp.given(values)
+    def check(v):
+        assert _cbor.loads(_cbor.dumps(v)) == v
+
+    check()
+
+
+def test_cbor_truncations_are_errors(pkg):
+    """Every proper prefix of an encoding is rejected, never misread."""
+    from tensor_net_gb300 import _cbor
+    from tensor_net_gb300.gates import Gate, Meas, Uni
+    from tensor_net_gb300 import circuits
+    v = [[circuits.uni_to_value(Uni.of_gate(Gate.U(1, 0.1, 0.2, 0.3))), circuits.meas_to_value(Meas.proj(2, 1))]]
+    b = _cbor.dumps(v)
+    for i in range(len(b)):
+        with pytest.raises(_cbor.CborError):
+            _cbor.loads(b[:i])
