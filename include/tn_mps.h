@@ -386,6 +386,13 @@ int tn_server_submit(tn_server *s, const tn_request *r, double arrival, uint64_t
 int tn_server_tick(tn_server *s, uint32_t *n_active, uint32_t *n_done);
 /* Completed requests (up to cap). */
 int tn_server_poll(tn_server *s, tn_result *out, uint32_t cap, uint32_t *n);
+/* Half-chain entropy after every layer of retired request `id` (the
+ * reference's per-trajectory output, entropy_vn(n/2 - 1) per layer), in
+ * layer order; *len = layers run.  With out = NULL only *len is set; a
+ * successful copy releases the record (each retired request's record is kept
+ * until fetched or the server is freed).  TN_NONE for an unknown or already
+ * fetched id. */
+int tn_server_history(tn_server *s, uint64_t id, double *out, uint32_t cap, uint32_t *len);
 /* Cancel request `id`.  A queued request is dropped at once; a resident one
  * is retired when the layer it is part of finishes (no kernel of the server
  * is using its memory after that), its slot and arena range freed.  Either

@@ -105,6 +105,7 @@ SIGNATURES = {
     "tn_server_tick": (C.c_int, [vp, P(u32), P(u32)]),
     "tn_server_poll": (C.c_int, [vp, P(tn_result), u32, P(u32)]),
     "tn_server_cancel": (C.c_int, [vp, u64]),
+    "tn_server_history": (C.c_int, [vp, u64, P(dbl), u32, P(u32)]),
     "tn_server_stats": (C.c_int, [vp, P(dbl)]),
     "tn_haar_u4": (C.c_int, [P(dbl), P(dbl)]),
     "tn_gen_layer": (C.c_int, [u64, u64, u32, u32, dbl, P(u32), P(dbl), P(u32), P(u32), P(dbl), P(u32)]),

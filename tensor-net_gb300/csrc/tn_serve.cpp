@@ -104,6 +104,7 @@ struct Active {
   size_t off = 0, bytes = 0;
   double entropy = 0;
   bool cancel = false;  // retire when the layer in flight finishes
+  std::vector<double> history;  // half-chain entropy after every layer
 };
 
 // One cost class: an engine (slots bound to arena memory), its queue, and
@@ -137,6 +138,7 @@ struct tn_server {
   int ncls = 1;
   int policy = 0;  // 0: first come, first served; 1: least estimated work first
   std::deque<tn_result> done;
+  std::map<uint64_t, std::vector<double>> histories;  // retired requests' entropies, until fetched
   uint64_t next_id = 1;
   double layers_done = 0, busy_s = 0, ticks = 0, admitted = 0, completed = 0;
   std::chrono::steady_clock::time_point t0;
@@ -213,6 +215,8 @@ int admit(tn_server *s, Class &c) {
     a.bytes = bytes;
     a.entropy = 0;
     a.cancel = false;
+    a.history.clear();
+    a.history.reserve(p.r.depth);
     s->admitted += 1;
     c.active += 1;
     c.pending.erase(c.pending.begin() + std::ptrdiff_t(pi));
@@ -277,6 +281,8 @@ void retire(tn_server *s, Class &c, uint32_t slot, int32_t status, double t_end)
   res.queue_s = a.t_admit - a.t_arrival;
   res.status = status;
   s->done.push_back(res);
+  s->histories[a.id] = std::move(a.history);
+  a.history.clear();
   s->alloc.release(a.off, a.bytes);
   a.on = false;
   a.cancel = false;
@@ -295,6 +301,7 @@ int collect(tn_server *s, Class &c, uint32_t *ndone) {
   for (uint32_t j = 0; j < nt; ++j) {
     Active &a = c.act[c.trajs[j]];
     a.entropy = c.ents[j];
+    a.history.push_back(a.entropy);
     a.layer += 1;
     if (a.layer >= a.r.depth) {
       retire(s, c, c.trajs[j], TN_OK, t_end);
@@ -461,6 +468,19 @@ int tn_server_stats(const tn_server *s, double *out) {
   out[5] = double(n_active(s));
   out[6] = s->admitted;
   out[7] = s->completed;
+  return TN_OK;
+}
+
+int tn_server_history(tn_server *s, uint64_t id, double *out, uint32_t cap, uint32_t *len) {
+  if (!s) return TN_ERR_INVALID_ARG;
+  auto it = s->histories.find(id);
+  if (it == s->histories.end()) return TN_NONE;
+  const uint32_t l = uint32_t(it->second.size());
+  if (len) *len = l;
+  if (!out) return TN_OK;
+  if (cap < l) return TN_ERR_INVALID_ARG;
+  std::copy(it->second.begin(), it->second.end(), out);
+  s->histories.erase(it);
   return TN_OK;
 }
 

@@ -54,12 +54,29 @@ class Server:
         L.check(self._lib.tn_server_tick(self._h, C.byref(a), C.byref(d)), "tn_server_tick")
         return int(a.value), int(d.value)
 
-    def poll(self, cap: int = 4096):
+    def poll(self, cap: int = 4096, history: bool = False):
+        """Retired requests; with ``history`` each result also carries
+        ``entropies``, the half-chain entropy after every layer
+        (``tn_server_history``)."""
         buf = (L.tn_result * cap)()
         n = L.u32()
         L.check(self._lib.tn_server_poll(self._h, buf, cap, C.byref(n)), "tn_server_poll")
-        return [dict(id=r.id, layers=r.layers, final_entropy=r.final_entropy, latency_s=r.latency_s,
-                     queue_s=r.queue_s, status=r.status) for r in buf[: n.value]]
+        out = [dict(id=r.id, layers=r.layers, final_entropy=r.final_entropy, latency_s=r.latency_s,
+                    queue_s=r.queue_s, status=r.status) for r in buf[: n.value]]
+        if history:
+            for d in out:
+                d["entropies"] = self.history(d["id"])
+        return out
+
+    def history(self, req_id: int):
+        ln = L.u32()
+        s = L.check(self._lib.tn_server_history(self._h, int(req_id), None, 0, C.byref(ln)), "tn_server_history")
+        if s == L.TN_NONE:
+            return None
+        buf = np.zeros(max(1, ln.value))
+        L.check(self._lib.tn_server_history(self._h, int(req_id), L.dptr(buf), buf.size, C.byref(ln)),
+                "tn_server_history")
+        return buf[: ln.value].copy()
 
     def cancel(self, req_id: int) -> bool:
         """Cancel a queued or resident request (``tn_server_cancel``); its

@@ -150,3 +150,26 @@ def test_cancel_queued_and_resident_requests(pkg):
         s2.tick()
         res = s2.poll()
     assert res[0]["id"] == i and res[0]["final_entropy"] == done[b]["final_entropy"]
+
+
+def test_per_layer_entropy_history_matches_a_batch(pkg):
+    """A served request's per-layer half-chain entropies (tn_server_history)
+    equal the same trajectory stepped in a batch and end at its final
+    entropy."""
+    reqs = _req_params()[:3]
+    s = pkg.Server(1 << 30, max_slots=4, precision="mixed", max_chi=32, max_n=16)
+    ids = {s.submit(r["n"], pkg.Trunc.both(r["chi"], 1e-10), r["p"], r["depth"], 99, r["traj"]): r for r in reqs}
+    got = {}
+    for _ in range(200):
+        s.tick()
+        for d in s.poll(history=True):
+            got[d["id"]] = d
+        if len(got) == len(reqs):
+            break
+    for i, r in ids.items():
+        h = got[i]["entropies"]
+        assert len(h) == r["depth"] and h[-1] == got[i]["final_entropy"]
+        b = pkg.Batch([r["n"]], [pkg.Trunc.both(r["chi"], 1e-10)], "mixed")
+        want = [b.step([0], [pkg.gen_layer(99, r["traj"], t, r["n"], r["p"])])[1][0] for t in range(r["depth"])]
+        np.testing.assert_allclose(h, want, rtol=0, atol=1e-6)
+        assert s.history(i) is None  # fetched once
