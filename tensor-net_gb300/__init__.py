@@ -8,7 +8,7 @@ This package is the host-side mirror of the reference API over that ABI.
 """
 from . import build
 from ._lib import STATUS, TN_CANCELLED as STATUS_CANCELLED, TnError, lib, library_path
-from . import circuits, gates
+from . import circuits, gates, layers
 from .batch import Batch
 from .coev import REFERENCE_BONDS, run_coevolution, run_coevolution_files, run_coevolution_layers
 from .gates import Gate, Meas, Uni
@@ -17,5 +17,5 @@ from .mps import MPS, Trunc
 from .serve import Server, poisson_requests, run_poisson
 
 __all__ = ["MPS", "Trunc", "Batch", "run_coevolution", "run_coevolution_files", "run_coevolution_layers",
-           "REFERENCE_BONDS", "TnError", "STATUS", "STATUS_CANCELLED", "lib", "library_path", "build", "circuits", "gates", "Gate", "Uni",
+           "REFERENCE_BONDS", "TnError", "STATUS", "STATUS_CANCELLED", "lib", "library_path", "build", "circuits", "gates", "layers", "Gate", "Uni",
            "Meas", "gen_layer", "gen_trajectory", "ginibre", "haar_u4", "Server", "poisson_requests", "run_poisson"]

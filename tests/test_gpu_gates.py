@@ -144,3 +144,42 @@ def test_layer_variants_multi_and_reset_match_the_oracle(pkg, ref):
     assert m.apply_op(g.Meas.proj(4, o)) == o
     assert m.apply_op(g.Uni.of_gate(g.Gate.H(0))) is None
     assert m.device_status() == 0
+
+
+def test_workspace_layer_drivers_match_the_oracle(pkg, ref):
+    """apply_main_layer(_probs) / apply_probe_layer (workspace/lib/haar.rs:
+    103-206): gates, then one measurement at a time with a full sweep each,
+    in list order; the oracle composed from the same single-site calls."""
+    from tensor_net_gb300 import layers
+    from tensor_net_gb300.gates import Meas
+    n = 8
+    m = pkg.MPS.new_qubits(n, pkg.Trunc.both(16, 1e-12), "f64")
+    r = ref.MPS(n, ref.Trunc.both(16, 1e-12))
+    for t in range(6):
+        gk, gs, _, _ = pkg.gen_layer(41, 0, t, n, 0.0)
+        unis = list(zip(gk, gs))
+        meas = [Meas.rand(5), Meas.proj(2, t % 2), Meas.rand(0)] if t % 2 else [Meas.rand(3)]
+        us = [0.41, 0.77][: sum(x.is_rand() for x in meas)]
+        outs, probs = layers.apply_main_layer_probs(m, unis, meas, us)
+        for k, u in unis:
+            r.apply_unitary2(int(k), u)
+        it = iter(us)
+        want = []
+        for x in meas:
+            if x.is_rand():
+                o, p = r.measure_prob(x.k, next(it))
+            else:
+                o, p = x.outcome, r.measure_postsel_prob(x.k, x.outcome)
+            want.append((x.k, o, p))
+        assert [(y.k, y.outcome) for y in outs] == [(k, o) for (k, o, _) in want]
+        for (k, p), (_, _, p2) in zip(probs, want):
+            assert abs(p - p2) < 1e-10
+    gk, gs, _, _ = pkg.gen_layer(41, 0, 6, n, 0.0)
+    outs, pr = layers.apply_probe_layer(m, list(zip(gk, gs)), [Meas.rand(1), Meas.rand(4)], target=4, us=[0.5])
+    for k, u in zip(gk, gs):
+        r.apply_unitary2(int(k), u)
+    o = r.measure(4, 0.5)
+    assert [(y.k, y.outcome) for y in outs] == [(4, o)]  # only the target's measurement, as the reference's filter
+    np.testing.assert_allclose(pr, r.probs(4), atol=1e-10)
+    for b in range(n - 1):
+        assert abs(m.entropy_vn(b) - r.entropy_vn(b)) < 1e-10
