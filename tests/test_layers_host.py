@@ -58,3 +58,38 @@ def test_probe_layer_keeps_only_the_target(pkg):
     st = FakeState()
     outs, pr = layers.apply_probe_layer(st, [], [Meas.rand(2), Meas.rand(4)], None, us=[0.1, 0.8])
     assert [(o.k, o.outcome) for o in outs] == [(2, 0), (4, 1)] and pr is None
+
+
+def _bare_mps(pkg, n, record):
+    """An MPS object without a device handle whose leaf methods record calls."""
+    m = object.__new__(pkg.MPS)
+    m._h = None
+    m.n = n
+
+    def aml(ks, us=None, posts=None):
+        record.append(("layer", list(ks), None if posts is None else list(posts)))
+        return [(k, p if p is not None else 0, 0.5) for k, p in zip(ks, posts or [None] * len(ks))]
+
+    m.apply_meas_prob_layer = aml
+    m.apply_unitary2 = lambda k, op: record.append(("u2", k, np.asarray(op)))
+    return m
+
+
+def test_postsel_layer_filter_and_multi_product(pkg):
+    rec = []
+    m = _bare_mps(pkg, 8, rec)
+    # invalid quantum numbers and sites are dropped before the de-duplication (mps.rs:1623-1635)
+    m.measure_postsel_prob_layer([(6, 2), (6, 1), (1, 0), (12, 0)])
+    assert rec[-1] == ("layer", [6, 1], [1, 0])
+    assert m.measure_postsel_prob_layer([(9, 0), (3, 5)]) == []
+    # apply_unitary2_multi multiplies ops[-1] ... ops[0] (mps.rs:1404-1413)
+    rng = np.random.default_rng(0)
+    ops = [rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4)) for _ in range(3)]
+    m.apply_unitary2_multi(2, ops)
+    np.testing.assert_allclose(rec[-1][2], ops[2] @ ops[1] @ ops[0])
+    n_before = len(rec)
+    m.apply_unitary2_multi(7, [np.eye(3)])  # out of range: nothing, not even the shape check
+    assert len(rec) == n_before
+    with pytest.raises(pkg.TnError):
+        m.apply_unitary2_multi(1, [np.eye(4), np.eye(2)])
+    assert len(rec) == n_before
