@@ -239,3 +239,57 @@ def test_oracle_from_vector_factorize():
     assert [len(s) for s in R.from_vector(ghz).svals] == [2] * (n - 1)
     one = R.from_vector(np.array([0.6, 0.8j]))
     assert one.n == 1 and np.allclose(one.data[0].reshape(-1), [0.6, 0.8j])
+
+
+def _two_time(state, mid_layers, x0, x1, post=None, us=None):
+    """One run of workspace/src/sampling_testing.rs:66-132 on a copy of
+    `state`: first layer, measurement of x0 (post-selected or sampled),
+    remaining layers, then probs / a sampled measurement of x1."""
+    s = state.copy()
+    for k, u in mid_layers[0]:
+        s.apply_unitary2(k, u)
+    if post is not None:
+        p0 = s.probs(x0)[post]
+        s.measure_postsel_prob(x0, post)
+        for layer in mid_layers[1:]:
+            for k, u in layer:
+                s.apply_unitary2(k, u)
+        return p0 * s.probs(x1)
+    a = s.measure(x0, us[0])
+    for layer in mid_layers[1:]:
+        for k, u in layer:
+            s.apply_unitary2(k, u)
+    return a, s.measure(x1, us[1])
+
+
+def test_sampling_exact_two_time_probabilities_match_monte_carlo():
+    """workspace/src/sampling_testing.rs: N=8, Const(6), 2N Haar layers, then
+    the two-time joint distribution of Z at N/2 (after one more layer) and Z
+    at N/2 (after two more): exact by post-selection, probabilities summing
+    to 1 within 1e-12, against a seeded Monte-Carlo of sampled measurements
+    (2000 runs, 5 sigma)."""
+    n, dt = 8, 2
+    x0 = x1 = n // 2
+    rng = np.random.default_rng(10546)
+
+    def layer(t):
+        return [(k, R.haar_from_ginibre(rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4))))
+                for k in R.tile_q2(n, t % 2 == 1)]
+
+    init = [layer(t) for t in range(2 * n)]
+    mid = [layer(t) for t in range(dt + 1)]
+    state = R.MPS(n, R.Trunc.const(6))
+    for lay in init:
+        for k, u in lay:
+            state.apply_unitary2(k, u)
+    exact = np.array([_two_time(state, mid, x0, x1, post=a) for a in (0, 1)])  # [a][b]
+    assert abs(exact.sum() - 1.0) < 1e-12
+    counts = np.zeros((2, 2))
+    runs = 2000
+    urng = np.random.default_rng(7)
+    for _ in range(runs):
+        a, b = _two_time(state, mid, x0, x1, us=urng.random(2))
+        counts[a, b] += 1
+    freq = counts / runs
+    sigma = np.sqrt(np.maximum(exact * (1 - exact), 1e-4) / runs)
+    assert np.all(np.abs(freq - exact) < 5 * sigma), (freq, exact)
