@@ -169,7 +169,11 @@ __global__ void k_fv_finish(const double2 *q, const double2 *r, double2 *qn, int
     const double snorm = sqrt(tot);
     // process_svd's rank rule on s / ||s|| (mps.rs:250-274)
     const bool has_cut = tr.trunc_mode == TN_TRUNC_CUTOFF || tr.trunc_mode == TN_TRUNC_BOTH;
-    const double eps = has_cut ? fabs(tr.cutoff) : 2.220446049250313e-16;
+    // values below the rounding noise of the rotated rows (about sqrt(len) eps
+    // relative) are not kept, as in the bond operations: an exact low-rank
+    // state would otherwise keep a noise value and divide Gamma by it
+    const double noise = 4.0 * sqrt(double(uint64_t(m) > nq ? uint64_t(m) : nq)) * 2.220446049250313e-16;
+    const double eps = fmax(has_cut ? fabs(tr.cutoff) : 2.220446049250313e-16, noise);
     // at most min(m, N) singular values, as a full SVD of the m x N matrix has
     const int lim = uint64_t(m) < nq ? m : int(nq);
     int lead = 0;
