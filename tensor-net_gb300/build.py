@@ -24,7 +24,9 @@ SO = LIBDIR / "libtnmps.so"
 STATIC = LIBDIR / "libtnmps.a"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
+# -ffp-contract=off: host arithmetic (the input generator) gives the same bits
+# on x86-64 and on aarch64, where gcc would otherwise fuse a*b + c into FMAs.
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           f"-I{INCLUDE}", f"-I{CSRC}"]
 
 
