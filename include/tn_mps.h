@@ -73,10 +73,14 @@ typedef struct {
 /* Arithmetic of the device path.  F64: complex128 Gamma, float64 Jacobi SVD
  * (the plain path).  MIXED: complex64 Gamma and theta, float32 Jacobi sweeps
  * accumulated in float32, float64 Lambda, renormalisation, rank decision,
- * probabilities and entropies. */
+ * probabilities and entropies.  DF: FP64-class results on the FP32 pipes --
+ * Gamma, theta and the Jacobi SVD in double-float arithmetic (pairs of float32,
+ * about 48 significant bits), float64 Lambda, renormalisation, rank decision,
+ * probabilities and entropies; the same 16 bytes per complex value as F64. */
 typedef enum {
     TN_PREC_F64 = 0,
-    TN_PREC_MIXED = 1
+    TN_PREC_MIXED = 1,
+    TN_PREC_DF = 2
 } tn_precision;
 
 typedef struct tn_mps tn_mps;
@@ -145,12 +149,15 @@ int tn_mps_apply_unitary2(tn_mps *m, uint32_t k, const double *op,
  * reference: for callers that cannot allocate device memory when they apply
  * a gate (a fixed memory plan that forbids allocation after start-up, or
  * work around a CUDA graph capture).  Same arguments and result as
- * tn_mps_apply_unitary2; the bond operation's scratch is a fixed 4 MiB
- * device array shared by every call (handles with chi capacity above 128 in
- * float64 or 256 in mixed precision are rejected with TN_ERR_CAPACITY).
+ * tn_mps_apply_unitary2 (a non-finite gate entry is TN_ERR_INVALID_ARG);
+ * the bond operation's scratch is a fixed 4.5 MiB device array shared by
+ * every call: handles with a chi capacity above 270 in mixed precision or
+ * above 191 in float64 / double-float are rejected with TN_ERR_CAPACITY.
  * Calls that overlap on the GPU race on that array: order them on one
- * stream.  The first call on a device looks up the array's address; make it
- * before any stream capture begins. */
+ * stream.  The gate is staged from host memory during the call, so the
+ * handle's stream must not be capturing (TN_ERR_INVALID_ARG).  The first
+ * call on a device looks up the array's address; make it before any stream
+ * capture begins. */
 int tn_mps_apply_unitary2_noalloc(tn_mps *m, uint32_t k, const double *op,
                                   uint32_t rows, uint32_t cols);
 
@@ -327,6 +334,11 @@ int tn_batch_set_tuning(tn_batch *b, int32_t scheme, int32_t max_sweeps);
  * gates of the layer as independent items) and the sweep launch (measurement
  * layers, refactor sweeps, entropy reads).  TN_NONE before any such step. */
 int tn_batch_last_launch_ms(tn_batch *b, float *gate_ms, float *sweep_ms);
+/* Device time (CUDA events on the batch stream) of the last tn_batch_step /
+ * tn_batch_step_post call from the end of its input copy to the start of its
+ * output copy: every kernel of the layer, with its inputs resident in HBM.
+ * TN_NONE before the first such step. */
+int tn_batch_last_step_device_ms(tn_batch *b, float *ms);
 /* Stream the batch launches on (a cudaStream_t), for callers that time with
  * CUDA events. */
 int tn_batch_stream(tn_batch *b, void **stream);

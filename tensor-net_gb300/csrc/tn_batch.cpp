@@ -95,6 +95,10 @@ struct tn_batch {
   bool ev_recorded = false;
   bool ev_one_launch = false;  // the recorded step ran the one-launch schedule
   cudaEvent_t ev_done = nullptr;  // end of the last host-input step (outputs in pinned memory)
+  // device interval of the last host-input step between its input copy and
+  // its output copy (every kernel of the step, inputs resident in HBM)
+  cudaEvent_t ev_step[2] = {nullptr, nullptr};
+  bool ev_step_recorded = false;
   uint32_t pending_nt = 0, pending_nm = 0;
   bool async_step = false;        // engine mode: tn_batch_step returns before the outputs arrive
   int grid_limit = 0;             // engine mode: CTAs per launch (0 = every resident CTA)
@@ -343,7 +347,7 @@ int tn_batch_create(uint32_t ntraj, const uint32_t *ns, const tn_trunc *truncs, 
                     const uint32_t *chi_caps, tn_batch **out) {
   if (!out || !ns || ntraj == 0) return TN_ERR_INVALID_ARG;
   *out = nullptr;
-  if (precision != TN_PREC_F64 && precision != TN_PREC_MIXED) return TN_ERR_INVALID_ARG;
+  if (precision != TN_PREC_F64 && precision != TN_PREC_MIXED && precision != TN_PREC_DF) return TN_ERR_INVALID_ARG;
   for (uint32_t i = 0; i < ntraj; ++i) {
     if (ns[i] == 0) return TN_ERR_EMPTY_SYSTEM;
     if (truncs && (truncs[i].mode < 0 || truncs[i].mode > 3)) return TN_ERR_INVALID_ARG;
@@ -357,7 +361,7 @@ int tn_batch_create(uint32_t ntraj, const uint32_t *ns, const tn_trunc *truncs, 
   b->cap.resize(ntraj);
   b->h.resize(ntraj);
   b->slot_bytes.resize(ntraj);
-  const size_t eb = precision == TN_PREC_F64 ? 16 : 8;
+  const size_t eb = prec_elem_bytes(precision);
   std::vector<size_t> off(ntraj);
   size_t total = 0;
   for (uint32_t i = 0; i < ntraj; ++i) {
@@ -390,6 +394,10 @@ int tn_batch_create(uint32_t ntraj, const uint32_t *ns, const tn_trunc *truncs, 
   }
   e = cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming);
   if (e != cudaSuccess) return bail(fail(e, "cudaEventCreate"));
+  for (auto &ev : b->ev_step) {
+    e = cudaEventCreate(&ev);
+    if (e != cudaSuccess) return bail(fail(e, "cudaEventCreate"));
+  }
   e = cudaMalloc(&b->arena, std::max<size_t>(total, 256));
   if (e != cudaSuccess) return bail(fail(e, "cudaMalloc(arena)"));
   e = cudaMalloc(reinterpret_cast<void **>(&b->dtraj), sizeof(TrajDev) * ntraj + sizeof(double) * STAT_N * ntraj +
@@ -462,6 +470,8 @@ int tn_batch_free(tn_batch *b) {
   for (auto &ev : b->ev)
     if (ev) cudaEventDestroy(ev);
   if (b->ev_done) cudaEventDestroy(b->ev_done);
+  for (auto &ev : b->ev_step)
+    if (ev) cudaEventDestroy(ev);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
   return TN_OK;
@@ -526,9 +536,9 @@ int tn_batch_import(tn_batch *b, uint32_t t, uint32_t n, const uint32_t *chi, co
     d.chi_max = 0;
     d.cutoff = 0.0;
   }
-  const size_t eb = b->prec == TN_PREC_F64 ? 16 : 8;
+  const size_t eb = prec_elem_bytes(b->prec);
   const size_t slot = size_t(2) * d.cap * d.cap * eb;
-  std::vector<float> tmp;
+  std::vector<char> tmp;
   size_t go = 0, lo = 0;
   for (uint32_t k = 0; k < n; ++k) {
     const size_t cnt = size_t(chi[k]) * 2 * chi[k + 1];
@@ -536,9 +546,9 @@ int tn_batch_import(tn_batch *b, uint32_t t, uint32_t n, const uint32_t *chi, co
     if (b->prec == TN_PREC_F64) {
       CKB(cudaMemcpy(dst, gammas + 2 * go, cnt * 16, cudaMemcpyHostToDevice));
     } else {
-      tmp.resize(2 * cnt);
-      for (size_t i = 0; i < 2 * cnt; ++i) tmp[i] = float(gammas[2 * go + i]);
-      CKB(cudaMemcpy(dst, tmp.data(), cnt * 8, cudaMemcpyHostToDevice));
+      tmp.resize(cnt * eb);
+      reals_to_layout(b->prec, gammas + 2 * go, 2 * cnt, tmp.data());
+      CKB(cudaMemcpy(dst, tmp.data(), tmp.size(), cudaMemcpyHostToDevice));
     }
     go += cnt;
     if (k + 1 < n) {
@@ -570,14 +580,14 @@ int tn_batch_export_gamma(tn_batch *b, uint32_t t, uint32_t k, double *out, uint
   if (!out) return TN_OK;
   const size_t cnt = size_t(c[0]) * 2 * c[1];
   if (cap < 2 * cnt) return TN_ERR_INVALID_ARG;
-  const size_t eb = b->prec == TN_PREC_F64 ? 16 : 8;
+  const size_t eb = prec_elem_bytes(b->prec);
   const char *src = static_cast<const char *>(d.gamma) + size_t(2) * d.cap * d.cap * eb * k;
   if (b->prec == TN_PREC_F64) {
     CKB(cudaMemcpy(out, src, cnt * 16, cudaMemcpyDeviceToHost));
   } else {
-    std::vector<float> tmp(2 * cnt);
-    CKB(cudaMemcpy(tmp.data(), src, cnt * 8, cudaMemcpyDeviceToHost));
-    for (size_t i = 0; i < 2 * cnt; ++i) out[i] = tmp[i];
+    std::vector<char> tmp(cnt * eb);
+    CKB(cudaMemcpy(tmp.data(), src, tmp.size(), cudaMemcpyDeviceToHost));
+    layout_to_reals(b->prec, tmp.data(), 2 * cnt, out);
   }
   return TN_OK;
 }
@@ -644,7 +654,10 @@ int tn_batch_step_post(tn_batch *b, const uint32_t *trajs, uint32_t nt, const ui
   StepPtrs P = ptrs_of(L, reinterpret_cast<char *>(b->dstep));
   P.order = nullptr;  // ranked on the device from the current bond dimensions
   P.posts = posts ? reinterpret_cast<const int *>(reinterpret_cast<char *>(b->dstep) + L.posts) : nullptr;
+  CKB(cudaEventRecord(b->ev_step[0], b->st));
   if (int s = launch_step(b, nt, P)) return s;
+  CKB(cudaEventRecord(b->ev_step[1], b->st));
+  b->ev_step_recorded = true;
   const size_t out_bytes = L.total - L.out_off;
   CKB(cudaMemcpyAsync(hb + L.out_off, reinterpret_cast<char *>(b->dstep) + L.out_off, out_bytes,
                       cudaMemcpyDeviceToHost, b->st));
@@ -857,6 +870,14 @@ int tn_batch_last_launch_ms(tn_batch *b, float *gate_ms, float *sweep_ms) {
   if (!b->ev_one_launch) CKB(cudaEventElapsedTime(&w, b->ev[1], b->ev[2]));
   if (gate_ms) *gate_ms = g;
   if (sweep_ms) *sweep_ms = w;
+  return TN_OK;
+}
+
+int tn_batch_last_step_device_ms(tn_batch *b, float *ms) {
+  if (!b || !ms) return TN_ERR_INVALID_ARG;
+  if (!b->ev_step_recorded) return TN_NONE;
+  CKB(cudaEventSynchronize(b->ev_step[1]));
+  CKB(cudaEventElapsedTime(ms, b->ev_step[0], b->ev_step[1]));
   return TN_OK;
 }
 

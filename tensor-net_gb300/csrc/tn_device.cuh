@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "tn_dd.cuh"
 #include "tn_internal.h"
 #include "tn_tc.cuh"
 
@@ -86,6 +87,97 @@ template <>
 struct Eps<float> {
   static constexpr float v = 1.1920929e-07f;
 };
+// rounding unit of the double-float operations (2^-47: the low float's own
+// rounding and the uncompensated cross terms of a product)
+template <>
+struct Eps<dd> {
+  static constexpr double v = 7.105427357601002e-15;
+};
+
+// Relative size (to ||A||_F = ||s||) below which a singular value is rounding
+// noise of the working precision: such vectors are neither rotated by the
+// Jacobi sweeps nor kept by the rank rule.  float and double: the rounding
+// level of a computed Gram entry (the rank rule uses 2 sqrt(ell) eps32 /
+// 4 sqrt(ell) eps64; the sweeps skip vectors below eps ||A||).  dd: the same
+// 4 sqrt(ell) eps rule, but never below 1e-12: the double-float pair has
+// float32's exponent range, so the Gram entries of vectors below that size
+// (|a_p||a_q| * tol < 1e-37) would reach float32's subnormal range and
+// could no longer be resolved to the tolerance.
+template <typename T>
+__host__ __device__ inline double rank_floor(int ell) {
+  return (sizeof(T) == 4 ? 2.0 : 4.0) * sqrt(double(ell)) * double(Eps<T>::v);
+}
+template <>
+__host__ __device__ inline double rank_floor<dd>(int ell) {
+  const double f = 4.0 * sqrt(double(ell)) * Eps<dd>::v;
+  return f > 1e-12 ? f : 1e-12;
+}
+template <typename T>
+__host__ __device__ inline double sweep_floor(int) {
+  return double(Eps<T>::v);
+}
+template <>
+__host__ __device__ inline double sweep_floor<dd>(int ell) {
+  return rank_floor<dd>(ell);
+}
+
+// Accumulators of sums of complex products.  For float and double the
+// accumulator is the complex value itself and acc_fin is the identity (the
+// arithmetic is exactly cfma / cjfma); for dd it is a pair of raw
+// accumulators (dacc) normalised once by acc_fin after the loop.
+template <typename T>
+struct CAcc {
+  using type = cpx<T>;
+};
+struct cdacc {
+  dacc x, y;
+};
+template <>
+struct CAcc<dd> {
+  using type = cdacc;
+};
+template <typename T>
+__device__ __forceinline__ typename CAcc<T>::type acc_zero() {
+  return czero<T>();
+}
+template <>
+__device__ __forceinline__ cdacc acc_zero<dd>() {
+  cdacc a;
+  a.x.hi = a.x.lo = a.y.hi = a.y.lo = 0.f;
+  return a;
+}
+// acc + a*b
+template <typename T>
+__device__ __forceinline__ void acc_fma(typename CAcc<T>::type &acc, cpx<T> a, cpx<T> b) {
+  acc = cfma(a, b, acc);
+}
+template <>
+__device__ __forceinline__ void acc_fma<dd>(cdacc &acc, cpx<dd> a, cpx<dd> b) {
+  dacc_add_prod(acc.x, a.x, b.x);
+  dacc_add_prod(acc.x, -a.y, b.y);
+  dacc_add_prod(acc.y, a.x, b.y);
+  dacc_add_prod(acc.y, a.y, b.x);
+}
+// acc + conj(a)*b
+template <typename T>
+__device__ __forceinline__ void acc_jfma(typename CAcc<T>::type &acc, cpx<T> a, cpx<T> b) {
+  acc = cjfma(a, b, acc);
+}
+template <>
+__device__ __forceinline__ void acc_jfma<dd>(cdacc &acc, cpx<dd> a, cpx<dd> b) {
+  dacc_add_prod(acc.x, a.x, b.x);
+  dacc_add_prod(acc.x, a.y, b.y);
+  dacc_add_prod(acc.y, a.x, b.y);
+  dacc_add_prod(acc.y, -a.y, b.x);
+}
+template <typename T>
+__device__ __forceinline__ cpx<T> acc_fin(const typename CAcc<T>::type &acc) {
+  return acc;
+}
+template <>
+__device__ __forceinline__ cpx<dd> acc_fin<dd>(const cdacc &acc) {
+  return mkc<dd>(dd_norm(acc.x.hi, acc.x.lo), dd_norm(acc.y.hi, acc.y.lo));
+}
 
 // --------------------------------------------------------- block helpers
 template <int NT>
@@ -319,11 +411,11 @@ __device__ void build_theta(const cpx<T> *__restrict__ gk, const cpx<T> *__restr
   const int tid = threadIdx.x;
   for (int v0 = 0; v0 < cL; v0 += TILE) {
     for (int w0 = 0; w0 < cR; w0 += TILE) {
-      cpx<T> acc[PER][4];
+      typename CAcc<T>::type acc[PER][4];
 #pragma unroll
       for (int e = 0; e < PER; ++e)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) acc[e][q] = czero<T>();
+        for (int q = 0; q < 4; ++q) acc[e][q] = acc_zero<T>();
       for (int u0 = 0; u0 < cM; u0 += TU) {
         __syncthreads();
         for (int idx = tid; idx < TILE * 2 * TU; idx += NT) {
@@ -349,10 +441,10 @@ __device__ void build_theta(const cpx<T> *__restrict__ gk, const cpx<T> *__restr
           for (int u = 0; u < TU; ++u) {
             cpx<T> x0 = Xs[(v * 2 + 0) * TU + u], x1 = Xs[(v * 2 + 1) * TU + u];
             cpx<T> y0 = Ys[(u * 2 + 0) * TILE + w], y1 = Ys[(u * 2 + 1) * TILE + w];
-            acc[e][0] = cfma(x0, y0, acc[e][0]);
-            acc[e][1] = cfma(x0, y1, acc[e][1]);
-            acc[e][2] = cfma(x1, y0, acc[e][2]);
-            acc[e][3] = cfma(x1, y1, acc[e][3]);
+            acc_fma<T>(acc[e][0], x0, y0);
+            acc_fma<T>(acc[e][1], x0, y1);
+            acc_fma<T>(acc[e][2], x1, y0);
+            acc_fma<T>(acc[e][3], x1, y1);
           }
         }
       }
@@ -365,7 +457,7 @@ __device__ void build_theta(const cpx<T> *__restrict__ gk, const cpx<T> *__restr
           const T sl = lamL[v], sr = lamR[w];
           cpx<T> th[4];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) th[q] = cscale(cscale(acc[e][q], sl), sr);
+          for (int q = 0; q < 4; ++q) th[q] = cscale(cscale(acc_fin<T>(acc[e][q]), sl), sr);
           if (gate) {
             cpx<T> t2[4];
 #pragma unroll
@@ -575,9 +667,9 @@ template <typename T, int NT, int W>
 __device__ void gram_stream(const cpx<T> *__restrict__ A, int ell, const int *cols, Smem<T, W> &sm) {
   constexpr int TP = W + 1;
   constexpr int PER = (W * W + NT - 1) / NT;
-  cpx<T> acc[PER];
+  typename CAcc<T>::type acc[PER];
 #pragma unroll
-  for (int e = 0; e < PER; ++e) acc[e] = czero<T>();
+  for (int e = 0; e < PER; ++e) acc[e] = acc_zero<T>();
   for (int i0 = 0; i0 < ell; i0 += 32) {
     __syncthreads();
     load_block_chunk<T, NT, W>(A, ell, cols, i0, sm.Ts);
@@ -588,8 +680,8 @@ __device__ void gram_stream(const cpx<T> *__restrict__ A, int ell, const int *co
       int o = threadIdx.x + e * NT;
       if (o < W * W) {
         int p = o / W, q = o % W;
-        cpx<T> a = acc[e];
-        for (int r = 0; r < rmax; ++r) a = cjfma(sm.Ts[r * TP + p], sm.Ts[r * TP + q], a);
+        typename CAcc<T>::type a = acc[e];
+        for (int r = 0; r < rmax; ++r) acc_jfma<T>(a, sm.Ts[r * TP + p], sm.Ts[r * TP + q]);
         acc[e] = a;
       }
     }
@@ -597,7 +689,7 @@ __device__ void gram_stream(const cpx<T> *__restrict__ A, int ell, const int *co
 #pragma unroll
   for (int e = 0; e < PER; ++e) {
     int o = threadIdx.x + e * NT;
-    if (o < W * W) sm.G[(o / W) * (W + 1) + o % W] = acc[e];
+    if (o < W * W) sm.G[(o / W) * (W + 1) + o % W] = acc_fin<T>(acc[e]);
   }
   __syncthreads();
 }
@@ -620,9 +712,9 @@ __device__ void update_stream(cpx<T> *__restrict__ X, int ld, int rows, const in
       if (o < 32 * W) {
         int q = o >> 5, r = o & 31;
         if (cols[q] >= 0) {
-          cpx<T> a = czero<T>();
-          for (int p = 0; p < W; ++p) a = cfma(sm.Ts[r * TP + p], Jm[p * (W + 1) + q], a);
-          out[e] = a;
+          typename CAcc<T>::type a = acc_zero<T>();
+          for (int p = 0; p < W; ++p) acc_fma<T>(a, sm.Ts[r * TP + p], Jm[p * (W + 1) + q]);
+          out[e] = acc_fin<T>(a);
         }
       }
     }
@@ -840,6 +932,57 @@ __device__ __forceinline__ bool jacobi_rotation<float>(float a, float b, cpx<flo
   return true;
 }
 
+// Whether the pair (a, b, g) of a Gram matrix needs a rotation: both
+// diagonals above the noise level and |g| > tol sqrt(a b).
+template <typename T>
+__device__ __forceinline__ bool pair_active(T a, T b, cpx<T> g, T tol, T tiny2) {
+  const T ag = sqrt(cabs2(g));
+  return a > tiny2 && b > tiny2 && ag > tol * sqrt(a) * sqrt(b);
+}
+
+// |g| of a dd complex value without squaring it (the square of a small Gram
+// entry would leave float32's range): the larger part times
+// sqrt(1 + (smaller / larger)^2); also the unit phase g / |g|.
+__device__ __forceinline__ dd dd_cabs(cpx<dd> g, cpx<dd> *phase) {
+  const dd gx = fabs(g.x), gy = fabs(g.y);
+  const bool xl = !(gx < gy);
+  const dd mx = xl ? gx : gy;
+  if (!(mx.hi > 0.f)) {
+    if (phase) *phase = mkc<dd>(dd(1.f, 0.f), dd(0.f, 0.f));
+    return dd(0.f, 0.f);
+  }
+  const dd ux = g.x / mx, uy = g.y / mx;  // components of g / max(|gx|, |gy|)
+  const dd r = sqrt(ux * ux + uy * uy);  // in [1, sqrt 2]
+  if (phase) *phase = mkc<dd>(ux / r, -(uy / r));
+  return mx * r;
+}
+
+template <>
+__device__ __forceinline__ bool pair_active<dd>(dd a, dd b, cpx<dd> g, dd tol, dd tiny2) {
+  if (!(a > tiny2 && b > tiny2)) return false;
+  // |g| / sqrt(a) / sqrt(b) > tol, divided step by step to stay in range
+  return (dd_cabs(g, nullptr) / sqrt(a)) / sqrt(b) > tol;
+}
+
+// The double-float rotation: the formulas of the generic version, with |g|
+// and the phase from dd_cabs and t = 1 / (2 |zeta|) once zeta^2 would
+// overflow float32 (|zeta| > 1e15, where sqrt(1 + zeta^2) = |zeta| to the
+// working precision).
+template <>
+__device__ __forceinline__ bool jacobi_rotation<dd>(dd a, dd b, cpx<dd> g, dd tol, dd tiny2, dd &c, dd &sn,
+                                                    cpx<dd> &e) {
+  if (!(a > tiny2 && b > tiny2)) return false;
+  const dd ag = dd_cabs(g, &e);
+  if (!((ag / sqrt(a)) / sqrt(b) > tol)) return false;
+  const dd zeta = (b - a) / (dd(2.f) * ag);
+  const dd az = fabs(zeta);
+  dd t_ = az.hi > 1e15f ? dd(0.5f) / az : dd(1.f) / (az + sqrt(dd(1.f) + az * az));
+  if (zeta.hi < 0.f) t_ = -t_;
+  c = dd(1.f) / sqrt(dd(1.f) + t_ * t_);
+  sn = t_ * c;
+  return true;
+}
+
 // One cyclic sweep of two-sided Jacobi on the Hermitian W x W matrix in
 // sm.G (row pitch W + 1) with round-robin ordering, accumulating J (same
 // pitch).  Warp t owns rotation pair t of every round: all its lanes compute
@@ -927,7 +1070,7 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
     fro += double(x.x * x.x + x.y * x.y);
   }
   fro = block_sum<NT>(fro, sm.red);
-  const T tiny2 = T(fro * double(Eps<T>::v) * double(Eps<T>::v));
+  const T tiny2 = T(fro * sweep_floor<T>(ell) * sweep_floor<T>(ell));
   const int nblk = (c + B - 1) / B;
   int *cols = sm.ired + 128;  // W ints (ired[0..128) is reduction scratch)
   // Column norms^2, kept current from the rotated Gram diagonals; each sweep
@@ -939,7 +1082,7 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
       T part = T(0);
       for (int i = lane; i < ell; i += 32) part += cabs2(A[size_t(j) * ell + i]);
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+      for (int o = 16; o > 0; o >>= 1) part += shfl_xor(part, o);
       if (lane == 0) nrm[j] = double(part);
     }
     __syncthreads();
@@ -1073,9 +1216,7 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
           const bool cross = (p < B) != (q < B);
           if (mode == 1 && !cross) continue;
           if (mode == 2 && cross) continue;
-          T a = sm.G[p * (W + 1) + p].x, b = sm.G[q * (W + 1) + q].x;
-          T ag = sqrt(cabs2(sm.G[p * (W + 1) + q]));
-          if (a > tiny2 && b > tiny2 && ag > tol * sqrt(a) * sqrt(b)) {
+          if (pair_active<T>(sm.G[p * (W + 1) + p].x, sm.G[q * (W + 1) + q].x, sm.G[p * (W + 1) + q], tol, tiny2)) {
             if (cross)
               needC = 1;
             else
@@ -1162,9 +1303,9 @@ __device__ void gemm_nt(int M, int N, int K, FP P, FQ Q, FE E, Smem<T, W> &sm) {
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;  // 16 x 32
   for (int x0 = 0; x0 < M; x0 += GT) {
     for (int y0 = 0; y0 < N; y0 += GT) {
-      cpx<T> acc[4][2];
+      typename CAcc<T>::type acc[4][2];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) acc[i][0] = acc[i][1] = czero<T>();
+      for (int i = 0; i < 4; ++i) acc[i][0] = acc[i][1] = acc_zero<T>();
       for (int k0 = 0; k0 < K; k0 += GK) {
         __syncthreads();
         for (int idx = threadIdx.x; idx < GK * GT; idx += NT) {
@@ -1185,7 +1326,7 @@ __device__ void gemm_nt(int M, int N, int K, FP P, FQ Q, FE E, Smem<T, W> &sm) {
 #pragma unroll
           for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int j = 0; j < 2; ++j) acc[i][j] = cfma(pv[i], qv[j], acc[i][j]);
+            for (int j = 0; j < 2; ++j) acc_fma<T>(acc[i][j], pv[i], qv[j]);
         }
       }
 #pragma unroll
@@ -1193,7 +1334,7 @@ __device__ void gemm_nt(int M, int N, int K, FP P, FQ Q, FE E, Smem<T, W> &sm) {
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
           int x = x0 + tx * 4 + i, y = y0 + ty * 2 + j;
-          if (x < M && y < N) E(x, y, acc[i][j]);
+          if (x < M && y < N) E(x, y, acc_fin<T>(acc[i][j]));
         }
     }
   }
@@ -1343,7 +1484,7 @@ __device__ void finalize_bond(const TrajDev &tr, int k, cpx<T> *__restrict__ gk,
   // included) and dividing by them (Gamma = U / Lambda) amplifies rounding,
   // so they are never kept.  The floor only matters for None/Const (the
   // reference's threshold is f64::EPSILON there); cutoffs >= 1e-12 are above it.
-  eps = fmax(eps, (sizeof(T) == 4 ? 2.0 : 4.0) * sqrt(double(ell)) * double(Eps<T>::v));
+  eps = fmax(eps, rank_floor<T>(ell));
   int firstbad = c;
   for (int j = threadIdx.x; j < c; j += NT) {
     double s = key[j] / norm1;

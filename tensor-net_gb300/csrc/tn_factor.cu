@@ -137,11 +137,25 @@ __global__ void k_fv_round(double2 *q, double2 *r, int m, int mp, uint64_t nq, i
   if (lane == 0) atomicOr(rotated, 1);
 }
 
+// Stores the complex value (re, im) as element i of a Gamma slot in the
+// layout of precision prec (0: complex128, 1: complex64, 2: double-float).
+__device__ void store_elem(void *gamma, int prec, size_t i, double re, double im) {
+  if (prec == 0) {
+    reinterpret_cast<double2 *>(gamma)[i] = make_double2(re, im);
+  } else if (prec == 2) {
+    const float rh = __double2float_rn(re), ih = __double2float_rn(im);
+    reinterpret_cast<float4 *>(gamma)[i] =
+        make_float4(rh, __double2float_rn(re - double(rh)), ih, __double2float_rn(im - double(ih)));
+  } else {
+    reinterpret_cast<float2 *>(gamma)[i] = make_float2(float(re), float(im));
+  }
+}
+
 __device__ bool fv_normal(double x) { return isfinite(x) && x != 0.0 && fabs(x) >= 2.2250738585072014e-308; }
 
 // Schmidt values, rank rule and the site's outputs (one CTA of 1024 threads).
 __global__ void k_fv_finish(const double2 *q, const double2 *r, double2 *qn, int m, uint64_t nq, int k,
-                            tn::TrajDev tr, int elem16, int *rank_out) {
+                            tn::TrajDev tr, int prec, int *rank_out) {
   __shared__ double sv[kFvMaxRows];
   __shared__ int perm[kFvMaxRows];
   __shared__ double s_snorm, s_norm2;
@@ -221,11 +235,7 @@ __global__ void k_fv_finish(const double2 *q, const double2 *r, double2 *qn, int
       vr /= l;
       vi /= l;
     }
-    if (elem16) {
-      reinterpret_cast<double2 *>(tr.gamma)[size_t(k) * slot + idx] = make_double2(vr, vi);
-    } else {
-      reinterpret_cast<float2 *>(tr.gamma)[size_t(k) * slot + idx] = make_float2(float(vr), float(vi));
-    }
+    store_elem(tr.gamma, prec, size_t(k) * slot + idx, vr, vi);
   }
   // next remainder: rows j < rank of R M, divided by ||s||
   const uint64_t total = uint64_t(rank) * nq;
@@ -238,7 +248,7 @@ __global__ void k_fv_finish(const double2 *q, const double2 *r, double2 *qn, int
 
 // Last site: Gamma_{n-1}[v, s, 0] = Q[v, s] / Lambda_{n-2}[v]; the edge
 // Lambdas and bond dimensions.  n == 1: Gamma_0 = psi.
-__global__ void k_fv_last(const double2 *q, int udim, int n, tn::TrajDev tr, int elem16) {
+__global__ void k_fv_last(const double2 *q, int udim, int n, tn::TrajDev tr, int prec) {
   const size_t slot = size_t(2) * tr.cap * tr.cap;
   const double *lam_prev = tr.lam + size_t(n - 1) * tr.cap;
   for (int idx = threadIdx.x; idx < 2 * udim; idx += blockDim.x) {
@@ -248,11 +258,7 @@ __global__ void k_fv_last(const double2 *q, int udim, int n, tn::TrajDev tr, int
       x.x /= l;
       x.y /= l;
     }
-    if (elem16) {
-      reinterpret_cast<double2 *>(tr.gamma)[size_t(n - 1) * slot + idx] = x;
-    } else {
-      reinterpret_cast<float2 *>(tr.gamma)[size_t(n - 1) * slot + idx] = make_float2(float(x.x), float(x.y));
-    }
+    store_elem(tr.gamma, prec, size_t(n - 1) * slot + idx, x.x, x.y);
   }
   if (threadIdx.x == 0) {
     tr.lam[0] = 1.0;
@@ -292,7 +298,6 @@ int factorize(const tn::TrajDev &tr, int prec, const double *state, uint64_t len
   double *dnorm = static_cast<double *>(sf.p);
   int *dflag = reinterpret_cast<int *>(dnorm + 1);
   int *drank = reinterpret_cast<int *>(dnorm + 2);
-  const int elem16 = prec == TN_PREC_F64 ? 1 : 0;
   FV_CK(cudaMemcpyAsync(qa, state, len * sizeof(double2), cudaMemcpyHostToDevice, st));
   k_fv_norm<<<1, 1024, 0, st>>>(qa, len, dnorm);
   FV_CK(cudaGetLastError());
@@ -323,7 +328,7 @@ int factorize(const tn::TrajDev &tr, int prec, const double *state, uint64_t len
       converged = flag == 0;
     }
     if (!converged) return TN_ERR_NOT_CONVERGED;
-    k_fv_finish<<<1, 1024, 0, st>>>(qa, rm, qb, m, nq, k, tr, elem16, drank);
+    k_fv_finish<<<1, 1024, 0, st>>>(qa, rm, qb, m, nq, k, tr, prec, drank);
     FV_CK(cudaGetLastError());
     int rank = 0;
     FV_CK(cudaMemcpyAsync(&rank, drank, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -332,7 +337,7 @@ int factorize(const tn::TrajDev &tr, int prec, const double *state, uint64_t len
     std::swap(qa, qb);
     udim = rank;
   }
-  k_fv_last<<<1, 256, 0, st>>>(qa, udim, n, tr, elem16);
+  k_fv_last<<<1, 256, 0, st>>>(qa, udim, n, tr, prec);
   FV_CK(cudaGetLastError());
   FV_CK(cudaStreamSynchronize(st));
   return TN_OK;

@@ -126,7 +126,7 @@ void fill_trunc(TrajDev &d, const tn_trunc *tr) {
   }
 }
 
-size_t elem_bytes(int prec) { return prec == TN_PREC_F64 ? 16 : 8; }
+size_t elem_bytes(int prec) { return prec_elem_bytes(prec); }
 
 // Host restatement of the measurement-layer control flow of
 // apply_meas_prob_layer (mps.rs:2206-2252): targets already filtered, sorted,
@@ -387,10 +387,10 @@ int read_gamma(const tn_mps *m, uint32_t k, const std::vector<int> &chi, std::ve
     CK(cudaMemcpyAsync(out.data(), src, cnt * 16, cudaMemcpyDeviceToHost, m->st));
     CK(cudaStreamSynchronize(m->st));
   } else {
-    std::vector<float> tmp(2 * cnt);
-    CK(cudaMemcpyAsync(tmp.data(), src, cnt * 8, cudaMemcpyDeviceToHost, m->st));
+    std::vector<char> tmp(cnt * elem_bytes(m->prec));
+    CK(cudaMemcpyAsync(tmp.data(), src, tmp.size(), cudaMemcpyDeviceToHost, m->st));
     CK(cudaStreamSynchronize(m->st));
-    for (size_t i = 0; i < 2 * cnt; ++i) out[i] = tmp[i];
+    layout_to_reals(m->prec, tmp.data(), 2 * cnt, out.data());
   }
   return TN_OK;
 }
@@ -421,7 +421,7 @@ int tn_mps_new_qubits(uint32_t n, const tn_trunc *trunc, int32_t precision, uint
   if (!out) return TN_ERR_INVALID_ARG;
   *out = nullptr;
   if (n == 0) return TN_ERR_EMPTY_SYSTEM;
-  if (precision != TN_PREC_F64 && precision != TN_PREC_MIXED) return TN_ERR_INVALID_ARG;
+  if (precision != TN_PREC_F64 && precision != TN_PREC_MIXED && precision != TN_PREC_DF) return TN_ERR_INVALID_ARG;
   if (int s = check_trunc(trunc)) return s;
   int cnt = 0;
   if (cudaGetDeviceCount(&cnt) != cudaSuccess || cnt == 0) {
@@ -532,7 +532,7 @@ int tn_mps_import(uint32_t n, const uint32_t *chi, const double *gammas, const d
   }
   const size_t slot = size_t(2) * m->cap * m->cap * elem_bytes(m->prec);
   std::vector<int> ichi(chi, chi + n + 1);
-  std::vector<float> tmp;
+  std::vector<char> tmp;
   cudaError_t e = cudaStreamSynchronize(m->st);
   size_t go = 0, lo = 0;
   for (uint32_t k = 0; k < n && e == cudaSuccess; ++k) {
@@ -541,9 +541,9 @@ int tn_mps_import(uint32_t n, const uint32_t *chi, const double *gammas, const d
     if (m->prec == TN_PREC_F64) {
       e = cudaMemcpy(dst, gammas + 2 * go, cnt * 16, cudaMemcpyHostToDevice);
     } else {
-      tmp.resize(2 * cnt);
-      for (size_t i = 0; i < 2 * cnt; ++i) tmp[i] = float(gammas[2 * go + i]);
-      e = cudaMemcpy(dst, tmp.data(), cnt * 8, cudaMemcpyHostToDevice);
+      tmp.resize(cnt * elem_bytes(m->prec));
+      reals_to_layout(m->prec, gammas + 2 * go, 2 * cnt, tmp.data());
+      e = cudaMemcpy(dst, tmp.data(), tmp.size(), cudaMemcpyHostToDevice);
     }
     go += cnt;
     if (e == cudaSuccess && k + 1 < n) {

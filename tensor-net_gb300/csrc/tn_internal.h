@@ -162,6 +162,37 @@ cudaStream_t batch_stream(tn_batch *b);
 // Record the text of a failed CUDA call for tn_last_error() (thread-local).
 void set_last_error(const char *what, cudaError_t e);
 
+// Device element layout of a precision: F64 complex128 (16 bytes), MIXED
+// complex64 (8 bytes), DF double-float complex (four floats re.hi, re.lo,
+// im.hi, im.lo: 16 bytes).
+inline size_t prec_elem_bytes(int prec) { return prec == 1 ? 8 : 16; }
+// n real parts (interleaved complex128) to the device layout of prec (dst
+// holds n * prec_elem_bytes(prec) / 2 bytes) and back.
+inline void reals_to_layout(int prec, const double *src, size_t n, void *dst) {
+  if (prec == 0) {
+    for (size_t i = 0; i < n; ++i) static_cast<double *>(dst)[i] = src[i];
+  } else if (prec == 2) {
+    float *d = static_cast<float *>(dst);
+    for (size_t i = 0; i < n; ++i) {
+      const float hi = float(src[i]);
+      d[2 * i] = hi;
+      d[2 * i + 1] = float(src[i] - double(hi));
+    }
+  } else {
+    for (size_t i = 0; i < n; ++i) static_cast<float *>(dst)[i] = float(src[i]);
+  }
+}
+inline void layout_to_reals(int prec, const void *src, size_t n, double *dst) {
+  if (prec == 0) {
+    for (size_t i = 0; i < n; ++i) dst[i] = static_cast<const double *>(src)[i];
+  } else if (prec == 2) {
+    const float *s = static_cast<const float *>(src);
+    for (size_t i = 0; i < n; ++i) dst[i] = double(s[2 * i]) + double(s[2 * i + 1]);
+  } else {
+    for (size_t i = 0; i < n; ++i) dst[i] = double(static_cast<const float *>(src)[i]);
+  }
+}
+
 inline int next_pow2(int x) {
   int p = 1;
   while (p < x) p <<= 1;

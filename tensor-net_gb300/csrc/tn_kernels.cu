@@ -145,15 +145,19 @@ __global__ void __launch_bounds__(NT, 1) k_run(LaunchArgs la, int sortP, int ws_
   }
 }
 
-__global__ void k_reset(TrajDev *trajs, const int *list, int count, int elem_bytes) {
+__global__ void k_reset(TrajDev *trajs, const int *list, int count, int prec) {
   const int t = list[blockIdx.x];
   const TrajDev tr = trajs[t];
   const size_t slot = size_t(2) * tr.cap * tr.cap;
   for (int k = threadIdx.x; k < tr.n; k += blockDim.x) {
-    if (elem_bytes == 16) {
+    if (prec == 0) {
       cpx<double> *g = reinterpret_cast<cpx<double> *>(tr.gamma) + size_t(k) * slot;
       g[0] = mkc<double>(1.0, 0.0);
       g[1] = mkc<double>(0.0, 0.0);
+    } else if (prec == 2) {
+      cpx<dd> *g = reinterpret_cast<cpx<dd> *>(tr.gamma) + size_t(k) * slot;
+      g[0] = mkc<dd>(dd(1.f, 0.f), dd(0.f, 0.f));
+      g[1] = mkc<dd>(dd(0.f, 0.f), dd(0.f, 0.f));
     } else {
       cpx<float> *g = reinterpret_cast<cpx<float> *>(tr.gamma) + size_t(k) * slot;
       g[0] = mkc<float>(1.f, 0.f);
@@ -421,15 +425,21 @@ static cudaError_t launch_run_t(const LaunchArgs &la, int grid, int sortP, int w
 
 cudaError_t launch_run(int prec, const LaunchArgs &la, int grid, int sortP, int ws_cap, cudaStream_t st) {
   if (prec == 0) return launch_run_t<double, kThreads, kBlockW>(la, grid, sortP, ws_cap, st);
+  if (prec == 2) return launch_run_t<dd, kThreads, kBlockW>(la, grid, sortP, ws_cap, st);
   return launch_run_t<float, kThreads, kBlockW>(la, grid, sortP, ws_cap, st);
 }
 
 size_t run_smem_bytes(int prec, int sortP) {
   if (prec == 0) return SmemLayout<double, kBlockW>::total(sortP);
+  if (prec == 2) return SmemLayout<dd, kBlockW>::total(sortP);
   return SmemLayout<float, kBlockW>::total(sortP);
 }
 
-size_t run_work_bytes(int prec, int cap) { return prec == 0 ? work_bytes<double>(cap) : work_bytes<float>(cap); }
+size_t run_work_bytes(int prec, int cap) {
+  if (prec == 0) return work_bytes<double>(cap);
+  if (prec == 2) return work_bytes<dd>(cap);
+  return work_bytes<float>(cap);
+}
 
 int run_blocks_per_sm(int prec, int sortP) {
   int nb = 0;
@@ -438,6 +448,9 @@ int run_blocks_per_sm(int prec, int sortP) {
   if (prec == 0) {
     ensure_run_smem<double, kThreads, kBlockW>(smem);
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_run<double, kThreads, kBlockW>, kThreads, smem);
+  } else if (prec == 2) {
+    ensure_run_smem<dd, kThreads, kBlockW>(smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_run<dd, kThreads, kBlockW>, kThreads, smem);
   } else {
     ensure_run_smem<float, kThreads, kBlockW>(smem);
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_run<float, kThreads, kBlockW>, kThreads, smem);
@@ -448,7 +461,7 @@ int run_blocks_per_sm(int prec, int sortP) {
 
 cudaError_t launch_reset(TrajDev *trajs, const int *list, int count, int prec, cudaStream_t st) {
   if (count <= 0) return cudaSuccess;
-  k_reset<<<count, 128, 0, st>>>(trajs, list, count, prec == 0 ? 16 : 8);
+  k_reset<<<count, 128, 0, st>>>(trajs, list, count, prec);
   return cudaGetLastError();
 }
 

@@ -15,9 +15,15 @@
 // and stay until the process exits.
 //
 // Limits and sharing:
-//  - the scratch holds kScratchBytes (4 MiB): enough for a bond capacity of
-//    chi <= 128 in float64 or chi <= 256 in mixed precision; larger handles
+//  - the scratch holds kScratchBytes (4.5 MiB): enough for a bond capacity
+//    of chi <= 270 in mixed precision (so every chi_max <= 256 of the
+//    workloads) and chi <= 191 in float64 or double-float; larger handles
 //    are rejected with TN_ERR_CAPACITY before anything is launched;
+//  - the gate is refused with TN_ERR_INVALID_ARG when an entry is not
+//    finite, before any device work, as tn_mps_apply_unitary2 does;
+//  - the gate, program and work item are staged from host memory that lives
+//    only during the call, so the handle's stream must not be capturing a
+//    CUDA graph (checked: TN_ERR_INVALID_ARG);
 //  - every call, on every stream and handle, uses the same arrays, and they
 //    keep the last call's contents.  The counter is cleared by each call;
 //    the scratch needs no clearing (each bond operation writes the parts it
@@ -26,6 +32,7 @@
 //  - the first call on a device looks up the arrays' device addresses
 //    (cudaGetSymbolAddress, with that device current); make that first call
 //    before any stream capture begins.
+#include <cmath>
 #include <cstring>
 #include <mutex>
 
@@ -34,7 +41,7 @@
 
 namespace {
 
-constexpr size_t kScratchBytes = size_t(4) << 20;
+constexpr size_t kScratchBytes = size_t(9) << 19;  // 4.5 MiB
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
@@ -94,13 +101,22 @@ extern "C" int tn_mps_apply_unitary2_noalloc(tn_mps *m, uint32_t k, const double
   // argument handling identical to tn_mps_apply_unitary2 (mps.rs:1332-1341)
   if (v.n == 1 || k >= uint32_t(v.n - 1)) return TN_OK;
   if (rows != 4 || cols != 4) return TN_ERR_OPERATOR_SHAPE;
+  for (int i = 0; i < 32; ++i)
+    if (!std::isfinite(op[i])) return TN_ERR_INVALID_ARG;
   const size_t need = tn::run_work_bytes(v.prec, v.cap);
   if (need > kScratchBytes) {
-    tn::set_last_error("tn_mps_apply_unitary2_noalloc: the handle's bond capacity needs more scratch than the 4 MiB "
-                       "fixed array (chi <= 128 in float64, chi <= 256 in mixed precision)",
+    tn::set_last_error("tn_mps_apply_unitary2_noalloc: the handle's bond capacity needs more scratch than the "
+                       "4.5 MiB fixed array (chi <= 270 in mixed precision, chi <= 191 in float64 or double-float)",
                        cudaSuccess);
     return TN_ERR_CAPACITY;
   }
+  cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+  cudaError_t ce = cudaStreamIsCapturing(v.st, &cap_status);
+  if (ce != cudaSuccess) {
+    tn::set_last_error("tn_mps_apply_unitary2_noalloc: cudaStreamIsCapturing", ce);
+    return TN_ERR_CUDA;
+  }
+  if (cap_status != cudaStreamCaptureStatusNone) return TN_ERR_INVALID_ARG;
   DeviceSymbols *s = nullptr;
   if (int st = setup_current_device(&s)) return st;
   const tn::Instr prog{tn::OP_GATE, int(k), 0, 0};

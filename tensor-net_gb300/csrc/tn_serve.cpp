@@ -148,7 +148,7 @@ struct tn_server {
 namespace {
 
 size_t footprint(const tn_server *s, const tn_request &r, uint32_t cap) {
-  const size_t eb = s->prec == TN_PREC_F64 ? 16 : 8;
+  const size_t eb = prec_elem_bytes(s->prec);
   return align256(size_t(2) * cap * cap * eb * r.n) + align256(sizeof(double) * size_t(cap) * (r.n + 1)) +
          align256(sizeof(int) * (r.n + 1));
 }
@@ -190,7 +190,7 @@ int admit(tn_server *s, Class &c) {
     c.free_slots.pop_back();
     TrajDev d{};
     char *base = static_cast<char *>(s->arena) + off;
-    const size_t eb = s->prec == TN_PREC_F64 ? 16 : 8;
+    const size_t eb = prec_elem_bytes(s->prec);
     d.gamma = base;
     d.lam = reinterpret_cast<double *>(base + align256(size_t(2) * cap * cap * eb * p.r.n));
     d.chi = reinterpret_cast<int *>(reinterpret_cast<char *>(d.lam) + align256(sizeof(double) * size_t(cap) * (p.r.n + 1)));
@@ -332,7 +332,7 @@ extern "C" {
 int tn_server_create_classes(uint64_t hbm_bytes, uint32_t max_slots, int32_t precision, uint32_t max_chi,
                              uint32_t max_n, uint32_t light_chi, uint32_t light_ctas, tn_server **out) {
   if (!out || hbm_bytes == 0 || max_slots == 0 || max_chi == 0 || max_n == 0) return TN_ERR_INVALID_ARG;
-  if (precision != TN_PREC_F64 && precision != TN_PREC_MIXED) return TN_ERR_INVALID_ARG;
+  if (precision != TN_PREC_F64 && precision != TN_PREC_MIXED && precision != TN_PREC_DF) return TN_ERR_INVALID_ARG;
   *out = nullptr;
   int cnt = 0, dev = 0, sms = 1;
   if (cudaGetDeviceCount(&cnt) != cudaSuccess || cnt == 0) return TN_ERR_NO_DEVICE;

@@ -15,7 +15,7 @@ import numpy as np
 from . import _lib as L
 
 MODE_NONE, MODE_CONST, MODE_CUTOFF, MODE_BOTH = 0, 1, 2, 3
-PRECISIONS = {"f64": 0, "mixed": 1}
+PRECISIONS = {"f64": 0, "mixed": 1, "df": 2}
 
 
 @dataclass(frozen=True)

@@ -2,7 +2,8 @@
 
 Tolerances: the F64 path must match the oracle to 1e-9 on Schmidt values,
 probabilities and entropies (both use float64; they differ only in the SVD
-algorithm: one-sided Jacobi vs LAPACK gesvd).  The MIXED path (complex64
+algorithm: one-sided Jacobi vs LAPACK gesvd), and so must the DF path
+(double-float arithmetic, about 48 significant bits).  The MIXED path (complex64
 Gamma, float32 Jacobi) is held to 1e-4 on the small cases here; its error at
 the benchmark sizes is measured and reported, not asserted.  Outcomes must be
 identical except where |p - u| < 1e-9 (a tie the two paths may break
@@ -16,7 +17,7 @@ from gates import CX, CXREV, CZ, H, xrot
 pytestmark = pytest.mark.gpu
 
 LN2 = np.log(2.0)
-TOL = {"f64": 1e-9, "mixed": 1e-4}
+TOL = {"f64": 1e-9, "mixed": 1e-4, "df": 1e-9}
 
 
 def _pair(pkg, ref, n, trunc_args, prec, chi_cap=0):
@@ -28,7 +29,7 @@ def _pair(pkg, ref, n, trunc_args, prec, chi_cap=0):
 
 # The MIXED path drops Schmidt values below 2*sqrt(ell)*eps32 (float32 noise
 # floor, ell <= 2*chi); compare spectra above this floor.
-FLOOR = {"f64": 0.0, "mixed": 1e-4}
+FLOOR = {"f64": 0.0, "mixed": 1e-4, "df": 0.0}
 
 
 def _assert_same_state(g, r, tol, floor=0.0):
@@ -41,7 +42,7 @@ def _assert_same_state(g, r, tol, floor=0.0):
         assert np.max(np.abs(g.probs(k) - r.probs(k))) < tol, k
 
 
-@pytest.mark.parametrize("prec", ["f64", "mixed"])
+@pytest.mark.parametrize("prec", ["f64", "mixed", "df"])
 def test_rotation_known_answer(pkg, prec):
     """workspace/src/rotation_testing.rs:13-38 on the GPU."""
     th = 3 * np.pi / 5
@@ -49,7 +50,7 @@ def test_rotation_known_answer(pkg, prec):
     m.apply_unitary1(2, xrot(th))
     m.apply_unitary2(2, CX)
     p0, p1 = np.cos(th / 2) ** 2, np.sin(th / 2) ** 2
-    tol = 1e-12 if prec == "f64" else 1e-6
+    tol = 1e-6 if prec == "mixed" else 1e-12
     for k in range(5):
         exp = [p0, p1] if k in (2, 3) else [1.0, 0.0]
         np.testing.assert_allclose(m.probs(k), exp, atol=tol)
@@ -59,9 +60,9 @@ def test_rotation_known_answer(pkg, prec):
     assert m.device_status() == 0 and m1.device_status() == 0
 
 
-@pytest.mark.parametrize("prec", ["f64", "mixed"])
+@pytest.mark.parametrize("prec", ["f64", "mixed", "df"])
 def test_bell_and_ghz(pkg, prec):
-    tol = 1e-12 if prec == "f64" else 1e-6
+    tol = 1e-6 if prec == "mixed" else 1e-12
     m = pkg.MPS.new_qubits(4, None, prec)
     m.apply_unitary1(0, H)
     m.apply_unitary2(0, CX)
@@ -105,7 +106,7 @@ def test_cluster_state(pkg, ref):
     np.testing.assert_allclose(g.contract(), r.contract(), atol=1e-12)
 
 
-@pytest.mark.parametrize("prec", ["f64", "mixed"])
+@pytest.mark.parametrize("prec", ["f64", "mixed", "df"])
 @pytest.mark.parametrize("n,chi,p,seed", [(8, 16, 0.3, 1), (10, 8, 0.2, 2), (9, 32, 0.15, 3)])
 def test_trajectory_parity(pkg, ref, prec, n, chi, p, seed):
     """Seeded Haar brickwork with measurements, layer by layer."""
@@ -198,16 +199,17 @@ def test_last_site_measurement_reference_behaviour(pkg, ref):
     assert abs(g.entropy_vn(n - 2) - LN2) < 1e-12
 
 
-def test_batch_matches_single_and_is_mix_independent(pkg, ref):
+@pytest.mark.parametrize("prec", ["f64", "df"])
+def test_batch_matches_single_and_is_mix_independent(pkg, ref, prec):
     """Each trajectory's result is the same alone and in a mixed batch
     (bit-identical: one CTA runs one trajectory with a fixed reduction order),
     and equals the single-state API."""
     specs = [(8, 16, 0.2), (11, 8, 0.3), (6, 4, 0.1), (9, 32, 0.25)]
     ns = [s[0] for s in specs]
     truncs = [pkg.Trunc.both(s[1], 1e-12) for s in specs]
-    mix = pkg.Batch(ns, truncs, "f64")
-    alone = pkg.Batch([ns[1]], [truncs[1]], "f64")
-    single = pkg.MPS.new_qubits(ns[1], truncs[1], "f64")
+    mix = pkg.Batch(ns, truncs, prec)
+    alone = pkg.Batch([ns[1]], [truncs[1]], prec)
+    single = pkg.MPS.new_qubits(ns[1], truncs[1], prec)
     rtraj = ref.MPS(ns[1], ref.Trunc.both(8, 1e-12))
     for t in range(8):
         layers = [pkg.gen_layer(77, i, t, s[0], s[2]) for i, s in enumerate(specs)]

@@ -43,8 +43,18 @@ def _oracle_run(args):
     return ents, recs, [s.copy() for s in m.svals]
 
 
-def _pool():
-    return ProcessPoolExecutor(max_workers=min(8, os.cpu_count() or 1), mp_context=mp.get_context("spawn"))
+def _single_thread_blas():
+    """One BLAS thread per oracle process (set before the workers are spawned,
+    since they read it when numpy loads): several processes each running a
+    BLAS pool the size of the machine on small SVDs oversubscribe the cores."""
+    for var in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[var] = "1"
+
+
+def _pool(workers=None):
+    _single_thread_blas()
+    n = workers or min(8, os.cpu_count() or 1)
+    return ProcessPoolExecutor(max_workers=n, mp_context=mp.get_context("spawn"))
 
 
 def _gpu_run(pkg, n, chi, cutoff, prec, trajs_layers):
