@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--chi", type=int, default=256)
     ap.add_argument("--cutoff", type=float, default=1e-10)
     ap.add_argument("--prefill", type=int, default=10)
-    ap.add_argument("--prec", default="mixed", choices=["mixed", "f64"])
+    ap.add_argument("--prec", default="df", choices=["df", "mixed", "f64"])
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--schedule", type=int, default=1, choices=[0, 1])
@@ -72,6 +72,7 @@ def parse():
     ap.add_argument("--large-seconds", type=float, default=300.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--plain-layers", type=int, default=1, help="timed layers of each plain trajectory")
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--serve-policy", default="least-work", choices=["fcfs", "least-work"])
     ap.add_argument("--serve-active-per-cta", type=int, default=2,
@@ -178,83 +179,89 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def ncu_traffic():
+def ncu_traffic(prec):
     """DRAM traffic of the executor kernel per algorithmic flop, from the
-    committed ncu summary of a full-size launch (profiles/k_run_traffic.json)."""
-    p = ROOT / "profiles" / "k_run_traffic.json"
+    committed ncu summary of its launches (profiles/k_run_traffic_<prec>.json)."""
+    p = ROOT / "profiles" / f"k_run_traffic_{prec}.json"
     if not p.exists():
         return None
     try:
-        return json.loads(p.read_text())
+        d = json.loads(p.read_text())
+        d.setdefault("source", f"profiles/{p.name}: DRAM bytes per algorithmic flop of the captured launches "
+                               f"(ncu), times this launch's algorithmic flops")
+        return d
     except Exception:
         return None
 
 
 # ----------------------------------------------------------- CPU (oracle)
-def _cpu_worker(args):
-    """Run the op list of one trajectory layer on a random saturated Vidal
-    MPS with the FP64 oracle until the time budget is spent; return
-    (elapsed, flops_done, flops_total)."""
-    import numpy as np
-    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
-    from oracle import mps_ref as R
-    n, chi, cutoff, ops, gates, budget, seed = args
-    rng = np.random.default_rng(seed)
-    dims = saturated_dims(n, chi)
-    m = R.MPS(n, R.Trunc.both(chi, cutoff))
-    full = [1] + dims + [1]
-    for k in range(n):
-        g = rng.normal(size=(full[k], 2, full[k + 1])) + 1j * rng.normal(size=(full[k], 2, full[k + 1]))
-        m.data[k] = g / np.linalg.norm(g)
-    for b in range(n - 1):
-        s = np.sort(rng.random(dims[b]))[::-1] + 1e-3
-        m.svals[b] = s / np.linalg.norm(s)
-    tot = sum(op_flops(full[k], full[k + 1], full[k + 2], gt) for k, gt in ops)
-    done = 0.0
-    gi = 0
-    t0 = time.perf_counter()
-    for k, is_gate in ops:
-        if time.perf_counter() - t0 > budget:
-            break
-        cl, cm, cr = m.data[k].shape[0], m.data[k].shape[2], m.data[k + 1].shape[2]
-        if is_gate:
-            m.apply_unitary2(k, gates[gi % len(gates)])
-            gi += 1
-        else:
-            m.local_refactor(k)
-        done += op_flops(cl, cm, cr, is_gate)
-    return time.perf_counter() - t0, done, tot
-
-
-def cpu_baseline(n, chi, cutoff, layers_by_traj, budget, cores=None):
-    """Oracle throughput on the host cores: one process per core (spawn, one
-    BLAS thread each, the reference's rayon-over-trajectories pattern), each
-    running the op list of one trajectory layer of the timed layers on a
-    saturated state for `budget` seconds; the traj-layer time is extrapolated
-    from the fraction of the layer's algorithmic flops completed."""
-    import multiprocessing as mp
-    import numpy as np
-    if cores is None:
-        cores = len(os.sched_getaffinity(0))
+def _ref_traj_worker(args):
+    """One trajectory of the benchmark workload with the FP64 oracle on one
+    core: the untimed layers [0, t_first) from |0...0>, then timed layers
+    from t_first on (each apply_bilayer plus its half-chain entropy read)
+    until `budget` seconds have passed, at least one whole layer.  Inputs
+    come from oracle.gen_ref, the GPU arm's generator restated in Python, so
+    this arm loads no library of the product."""
+    root, n, chi, cutoff, seed, traj, p, t_first, budget = args
     os.environ["OPENBLAS_NUM_THREADS"] = "1"
     os.environ["OMP_NUM_THREADS"] = "1"
-    jobs = []
-    for i in range(cores):
-        gk, g, mk, us = layers_by_traj[i % len(layers_by_traj)]
-        ops = layer_ops(n, gk, mk)
-        jobs.append((n, chi, cutoff, ops, [np.asarray(x) for x in g] or [np.eye(4, dtype=complex)], budget, 1000 + i))
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_worker, jobs)
-    per_layer = [el / (done / tot) for el, done, tot in res if done > 0]
-    layer_s = statistics.mean(per_layer)
-    value = cores / layer_s
-    return {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": (f"FP64 oracle (numpy, LAPACK gesvd, 1 BLAS thread/process) on {cores} processes, each "
-                       f"running the bond-op list of one timed traj-layer (N={n}, chi_max={chi}, saturated "
-                       f"bond dims) for {budget:.0f} s; traj-layer time extrapolated from the fraction of its "
-                       f"algorithmic flops completed ({statistics.mean([d / t for _, d, t in res]):.3f} avg)"),
-            "seconds_per_traj_layer": layer_s}
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    from oracle import gen_ref as G
+    from oracle import mps_ref as R
+    m = R.MPS(n, R.Trunc.both(chi, cutoff))
+    t0 = time.perf_counter()
+    for t in range(t_first):
+        R.apply_bilayer(m, *G.gen_layer(seed, traj, t, n, p))
+    prep = time.perf_counter() - t0
+    times, t = [], t_first
+    start = time.perf_counter()
+    while True:
+        lay = G.gen_layer(seed, traj, t, n, p)
+        a0 = time.perf_counter()
+        R.apply_bilayer(m, *lay)
+        m.entropy_vn(n // 2 - 1)
+        times.append(time.perf_counter() - a0)
+        t += 1
+        if time.perf_counter() - start >= budget:
+            break
+    return {"traj": traj, "p": p, "prep_s": prep, "layer_s": times,
+            "mid_bond_dim": int(len(m.svals[n // 2 - 1]))}
+
+
+def reference_jobs(n, chi, cutoff, seed, t_first, budget, cores):
+    return [(str(ROOT), n, chi, cutoff, seed, i, p_of(i), t_first, budget) for i in range(cores)]
+
+
+def summarize_reference(res, t_first, budget):
+    """Throughput of the per-trajectory oracle processes: the sum over
+    processes of timed layers / time."""
+    cores = len(res)
+    rate = sum(len(r["layer_s"]) / sum(r["layer_s"]) for r in res)
+    layers = sum(len(r["layer_s"]) for r in res)
+    mean_layer = statistics.mean(x for r in res for x in r["layer_s"])
+    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": (f"FP64 oracle (numpy + LAPACK gesvd, 1 BLAS thread per process) on {cores} processes; "
+                       f"process i runs trajectory i of the GPU batch (p cycling {list(P_LIST)}) from |0...0> "
+                       f"through layers [0, {t_first}) untimed, then times whole layers from layer {t_first} "
+                       f"on for {budget:.0f} s ({layers} traj-layers timed, at least one per process)"),
+            "seconds_per_traj_layer_per_core": mean_layer,
+            "per_process": [{"traj": r["traj"], "p": r["p"], "layers": len(r["layer_s"]),
+                             "mean_layer_s": statistics.mean(r["layer_s"]), "prep_s": r["prep_s"],
+                             "mid_bond_dim": r["mid_bond_dim"]} for r in res]}
+
+
+def reference_arm(n, chi, cutoff, seed, t_first, budget, cores):
+    """The CPU arm on the same workload as the GPU arm: `cores` spawned
+    processes (one BLAS thread each, the reference's rayon-over-trajectories
+    pattern), process i running batch trajectory i (p cycling) from |0...0>
+    to the GPU arm's first timed layer untimed, then timing whole layers."""
+    import multiprocessing as mp
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    os.environ["OMP_NUM_THREADS"] = "1"
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(_ref_traj_worker, reference_jobs(n, chi, cutoff, seed, t_first, budget, cores))
+    return summarize_reference(res, t_first, budget)
 
 
 # --------------------------------------------------------------- GPU arm
@@ -278,9 +285,24 @@ def whole_job_rate(units_per_rank: int, steps: int, world: int, elapsed_max: flo
 # per-phase SM cycles of the bond operations, counted on the device (one CTA each)
 CYC_KEYS = ("cyc_theta", "cyc_gram", "cyc_rot", "cyc_update", "cyc_final")
 
+# Measured half-chain entropy error of each precision mode against the FP64
+# oracle on identical inputs (tests/test_gpu_precision.py: N=32, chi_max=64,
+# cutoff 1e-10, depth 64, one trajectory per p in P_LIST).
+PRECISION_NOTE = {
+    "df": "held below 1e-6 per p by tests/test_gpu_precision.py (N=32 chi_max=64 depth 64)",
+    "f64": "below 1e-12 (tests/test_gpu_parity.py, tests/test_gpu_workloads.py)",
+    "mixed": "1e-5 .. 2e-3 over p in {0.05..0.30} (does not meet the 1e-6 bound)",
+}
+
 
 def run_gpu(a, rank, world, local_rank):
-    import numpy as np
+    """The GPU arm.  Every layer goes through the library's public C ABI with
+    host buffers (tn_batch_step: one pinned H2D of the layer's gates and
+    uniforms, the layer's kernels, one D2H of outcomes, probabilities and
+    entropies).  Of the same K timed layers, `value` counts the device time
+    between each layer's input copy and output copy (CUDA events on the batch
+    stream: every kernel of the layer with its inputs resident in HBM) and
+    `e2e` the host wall time of the whole calls, copies included."""
     import torch
     import __graft_entry__ as ge
     pkg = ge.load_package()
@@ -304,37 +326,18 @@ def run_gpu(a, rank, world, local_rank):
         return [pkg.gen_layer(a.seed, traj0 + i, t, n, p_of(traj0 + i)) for i in range(B)]
 
     trajs = list(range(B))
-    # prefill (untimed): evolve from |0...0>
-    for t in range(a.prefill):
+    t_first = a.prefill + a.warmup
+    untimed_ms = []
+    for t in range(t_first):  # prefill and warm-up layers (untimed)
+        t0 = time.perf_counter()
         batch.step(trajs, layer_inputs(t))
-    # stage W + K layers of inputs in HBM
-    dev = torch.device("cuda", local_rank)
-    staged = []
-    for t in range(a.prefill, a.prefill + a.warmup + a.steps):
-        pk = batch.pack(trajs, layer_inputs(t))
-        nm = int(pk["meas_off"][-1])
-        staged.append(dict(
-            trajs=torch.as_tensor(pk["trajs"].astype(np.int32), device=dev),
-            gate_off=torch.as_tensor(pk["gate_off"].astype(np.int32), device=dev),
-            gate_ks=torch.as_tensor(np.maximum(pk["gate_ks"], 0).astype(np.int32), device=dev),
-            gates=torch.as_tensor(pk["gates"], device=dev),
-            meas_off=torch.as_tensor(pk["meas_off"].astype(np.int32), device=dev),
-            meas_ks=torch.as_tensor(pk["meas_ks"].astype(np.int32), device=dev) if nm else
-            torch.zeros(1, dtype=torch.int32, device=dev),
-            us=torch.as_tensor(pk["us"], device=dev) if nm else torch.zeros(1, dtype=torch.float64, device=dev),
-            outc=torch.zeros(max(nm, 1), dtype=torch.int32, device=dev),
-            probs=torch.zeros(max(nm, 1), dtype=torch.float64, device=dev),
-            ents=torch.zeros(B, dtype=torch.float64, device=dev)))
-    stream = torch.cuda.ExternalStream(batch.stream(), device=dev)
-
-    def launch(s):
-        batch.step_ptrs(B, s["trajs"].data_ptr(), None, s["gate_off"].data_ptr(),
-                        s["gate_ks"].data_ptr(), s["gates"].data_ptr(), s["meas_off"].data_ptr(),
-                        s["meas_ks"].data_ptr(), s["us"].data_ptr(), s["outc"].data_ptr(),
-                        s["probs"].data_ptr(), s["ents"].data_ptr())
-
-    for s in staged[: a.warmup]:
-        launch(s)
+        untimed_ms.append(1e3 * (time.perf_counter() - t0))
+    # the plain path starts from the same states (checkpoint export / import)
+    plain_states = []
+    if rank == 0 and world == 1 and not a.no_plain:
+        for i in range(min(len(P_LIST), B)):
+            plain_states.append(batch.export_parts(i))
+    packs = [batch.pack(trajs, layer_inputs(t)) for t in range(t_first, t_first + a.steps)]
     batch.synchronize()
     torch.cuda.synchronize()
     if world > 1:
@@ -342,69 +345,47 @@ def run_gpu(a, rank, world, local_rank):
     batch.stats(reset=True)
     clocks = ClockSampler(local_rank)
     clocks.start()
-    evs = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps + 1)]
-    split = []
-    with torch.cuda.stream(stream):
-        evs[0].record(stream)
-        for i, s in enumerate(staged[a.warmup:]):
-            launch(s)
-            evs[i + 1].record(stream)
-            split.append(batch.last_launch_ms())
+    dev_ms, host_s, split = [], [], []
+    t_all = time.perf_counter()
+    for pk in packs:
+        t0 = time.perf_counter()
+        batch.step_packed(pk)  # returns with the layer's outputs in host memory
+        host_s.append(time.perf_counter() - t0)
+        dev_ms.append(batch.last_step_device_ms())
+        split.append(batch.last_launch_ms())
     batch.synchronize()
     torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t_all
     clk = clocks.stop()
-    step_ms = [evs[i].elapsed_time(evs[i + 1]) for i in range(a.steps)]
-    elapsed = sum(step_ms) / 1e3
+    elapsed = sum(dev_ms) / 1e3
     st = batch.stats(reset=True)
     status = batch.device_status()
-    elapsed = max_over_ranks(elapsed, dev)
-    value = whole_job_rate(B, a.steps, world, elapsed)
-    ents = staged[-1]["ents"].cpu().numpy()
-
-    dims = [batch.bond_dims(i) for i in range(min(B, 5))]
-    batch.close()
-
-    # e2e: the same timed layers from the same state, through the C ABI with host
-    # buffers (pinned staging, H2D + launch + D2H per step).  A second batch
-    # replays the untimed prefill and warm-up layers (bit-identical states), so
-    # that both numbers describe the same work.
-    b2 = pkg.Batch([n] * B, [trunc] * B, a.prec)
-    b2.set_schedule(a.schedule)
-    b2.set_theta_path(a.theta == "simt")
-    if a.scheme is not None:
-        b2.set_tuning(a.scheme, 40)
-    for t in range(a.prefill + a.warmup):
-        b2.step(trajs, layer_inputs(t))
-    packs = [b2.pack(trajs, layer_inputs(t)) for t in range(a.prefill + a.warmup, a.prefill + a.warmup + a.steps)]
-    b2.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    t0 = time.perf_counter()
-    for pk in packs:
-        b2.step_packed(pk)
-    e2e_s = time.perf_counter() - t0
-    e2e_s = max_over_ranks(e2e_s, dev)
+    elapsed = max_over_ranks(elapsed, torch.device("cuda", local_rank))
+    e2e_s = max_over_ranks(e2e_s, torch.device("cuda", local_rank))
     h2d = statistics.mean(int(pk["gates"].nbytes + pk["us"].nbytes + 4 * (pk["gate_ks"].size + pk["meas_ks"].size +
                                                                          2 * B + 2 * (B + 1))) for pk in packs)
     d2h = statistics.mean(int(int(pk["meas_off"][-1]) * (4 + 8) + 8 * B) for pk in packs)
-    b2.close()
-    return dict(value=value, elapsed=elapsed, step_ms=step_ms, split=split, stats=st, status=status, clocks=clk,
+    dims = [batch.bond_dims(i) for i in range(min(B, 5))]
+    batch.close()
+    return dict(value=whole_job_rate(B, a.steps, world, elapsed), elapsed=elapsed, step_ms=dev_ms,
+                host_step_s=host_s, split=split, untimed_ms=untimed_ms, stats=st, status=status, clocks=clk,
                 e2e=whole_job_rate(B, a.steps, world, e2e_s), h2d=h2d, d2h=d2h, B=B, gpu=name.value.decode(),
-                ents=ents, dims=dims, sms=int(sms.value), layer_inputs=layer_inputs)
+                dims=dims, sms=int(sms.value), plain_states=plain_states)
 
 
-def run_plain(a, pkg):
+def run_plain(a, pkg, states):
     """The plain path: one trajectory at a time through the single-state API
-    (tn_mps_apply_bilayer + entropy read), on the same inputs as batch
-    trajectories 0..4 (one per p), timed on the same layer indices."""
+    (tn_mps_apply_bilayer + entropy read, host-timed), on batch trajectories
+    0..4 (one per p) from the states they had at the first timed layer
+    (exported from the batch and imported into single-state handles), over
+    `--plain-layers` of the timed layers."""
     t_lo = a.prefill + a.warmup
+    nl = min(a.plain_layers, a.steps)
     total, layers = 0.0, 0
-    for i in range(len(P_LIST)):
-        m = pkg.MPS.new_qubits(a.n, pkg.Trunc.both(a.chi, a.cutoff), a.prec)
-        for t in range(t_lo):
-            m.apply_bilayer(*pkg.gen_layer(a.seed, i, t, a.n, p_of(i)))
+    for i, (gammas, lams) in enumerate(states):
+        m = pkg.MPS.from_parts(gammas, lams, pkg.Trunc.both(a.chi, a.cutoff), a.prec, a.chi)
         m.entropy_vn(a.n // 2 - 1)
-        for t in range(t_lo, t_lo + a.steps):
+        for t in range(t_lo, t_lo + nl):
             inp = pkg.gen_layer(a.seed, i, t, a.n, p_of(i))
             t0 = time.perf_counter()
             m.apply_bilayer(*inp)
@@ -413,8 +394,9 @@ def run_plain(a, pkg):
             layers += 1
         m.close()
     return {"value": layers / total, "unit": UNIT,
-            "how": f"single-state API, one trajectory at a time, {layers} traj-layers (one trajectory per p, "
-                   f"layers [{t_lo}, {t_lo + a.steps})), host-timed"}
+            "how": f"single-state API (one trajectory at a time), {layers} traj-layers: trajectories "
+                   f"0..{len(states) - 1} (one per p) from their batch states at layer {t_lo}, layers "
+                   f"[{t_lo}, {t_lo + nl}), host-timed"}
 
 
 def run_serving(a, pkg):
@@ -747,36 +729,31 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    config = {"workload": f"N={a.n} chi_max={a.chi} cutoff={a.cutoff:g} Haar brickwork, p cycling "
-                          f"{list(P_LIST)}, layers [{a.prefill + a.warmup}, {a.prefill + a.warmup + a.steps}) "
-                          f"after {a.prefill} untimed prefill layers",
-              "n_qubits": a.n, "chi_max": a.chi, "cutoff": a.cutoff, "prefill_layers": a.prefill,
-              "precision": a.prec, "l2": "state larger than L2 (no flush needed)"}
+    t_first = a.prefill + a.warmup
+    config = {"workload": f"N={a.n} chi_max={a.chi} cutoff={a.cutoff:g} Haar brickwork from |0...0>, p cycling "
+                          f"{list(P_LIST)} over the trajectories, timed layers [{t_first}, {t_first + a.steps}) "
+                          f"after {a.prefill} untimed and {a.warmup} warm-up layers",
+              "n_qubits": a.n, "chi_max": a.chi, "cutoff": a.cutoff, "p_cycle": list(P_LIST),
+              "first_timed_layer": t_first, "timed_layers": a.steps, "seed": a.seed,
+              "l2": "state larger than L2 (no flush needed)"}
 
     if a.impl == "reference":
         if rank != 0:
             return
-        import numpy as np
-        sys.path.insert(0, str(ROOT))
-        import __graft_entry__ as ge
-        pkg = ge.load_package()
-        t = a.prefill + a.warmup
-        layers = [pkg.gen_layer(a.seed, i, t, a.n, p_of(i)) for i in range(16)]
-        steps = []
-        for _ in range(a.warmup + a.steps):
-            steps.append(cpu_baseline(a.n, a.chi, a.cutoff, layers, max(3.0, a.cpu_seconds / 2)))
-        cb = steps[-1]
-        vals = [s["value"] for s in steps[a.warmup:]]
-        v = statistics.mean(vals)
+        cores = len(os.sched_getaffinity(0))
+        cb = reference_arm(a.n, a.chi, a.cutoff, a.seed, t_first, a.cpu_seconds, cores)
+        v = cb["value"]
         out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus,
-               "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 / v if v else None,
+               "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * cb["seconds_per_traj_layer_per_core"],
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
                "data": "synthetic (seeded Haar gates and measurement uniforms)", "config": config,
-               "cpu_baseline": {"value": v, "unit": UNIT, "cores": cb["cores"], "kind": "port",
-                                "sample": cb["sample"]},
+               "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-               "note": "the reference is Rust (tensor-net); no Rust toolchain on these machines, so the "
-                       "reference arm is its FP64 restatement (oracle/mps_ref.py) on the host cores"}
+               "per_process": cb["per_process"],
+               "note": "the reference is Rust (tensor-net) and no Rust toolchain exists on these machines, so the "
+                       "reference arm is its FP64 restatement (oracle/mps_ref.py, LAPACK gesvd as the reference's "
+                       "ndarray-linalg svd_into) on the host cores; a step here is one traj-layer per process "
+                       "(ms_per_step = mean seconds per traj-layer on one core)"}
         print(json.dumps(out), flush=True)
         return
 
@@ -792,42 +769,62 @@ def main():
         print(json.dumps(out), flush=True)
         return
 
+    cpu_pool = cpu_async = None
+    if rank == 0 and world == 1 and not a.no_cpu:
+        # The CPU baseline runs on the host cores while the GPU works (the GPU
+        # arm's host thread only issues and waits; two cores are left to it and
+        # to the clock sampler): spawned processes, started before any GPU call.
+        import multiprocessing as mp
+        cores = max(1, len(os.sched_getaffinity(0)) - 2)
+        os.environ["OPENBLAS_NUM_THREADS"] = "1"
+        cpu_pool = mp.get_context("spawn").Pool(cores)
+        cpu_async = cpu_pool.map_async(_ref_traj_worker,
+                                       reference_jobs(a.n, a.chi, a.cutoff, a.seed, t_first, a.cpu_seconds, cores))
+
     import torch
     if world > 1:
         torch.distributed.init_process_group("nccl")
     r = run_gpu(a, rank, world, local_rank)
     peaks, peaks_kind = measured_peaks()
     flops = r["stats"]["flop_theta"] + r["stats"]["flop_svd"]
+    launch_ms = [x[0] + x[1] for x in r["split"] if x]
+    launch_s = sum(launch_ms) / 1e3 / max(1, len(launch_ms))
     per_launch = flops / a.steps
-    launch_s = r["elapsed"] / a.steps
     achieved = per_launch / launch_s / 1e12
     peak = float(peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops"))
-    tr = ncu_traffic()
     sm_mhz = r["clocks"].get("sm_mhz") or 2070.0
     cyc_sum = sum(r["stats"][k] for k in CYC_KEYS)
     simt_peak = r["sms"] * 128 * 2 * sm_mhz * 1e6 / 1e12
+    alg_bytes = r["stats"]["bytes"] / a.steps
+    tr = ncu_traffic(a.prec)
+    dtype = {"mixed": "c64+f64", "f64": "c128", "df": "df64 (float32 pairs) + f64"}[a.prec]
     out = {
         "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": r["elapsed"] / a.steps * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c64+f64" if a.prec == "mixed" else "c128",
+        "scaling": "weak", "vs_baseline": None, "dtype": dtype,
         "data": "synthetic (seeded Haar gates and measurement uniforms)",
-        "config": dict(config, batch_per_gpu=r["B"], gpu=r["gpu"]),
-        "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
+        "config": config,
+        "precision": {"mode": a.prec, "entropy_err_vs_fp64_oracle": PRECISION_NOTE.get(a.prec)},
+        "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"],
+                "how": "the same K layers as value, host wall time of tn_batch_step (pinned H2D + kernels + D2H)"},
         # per timed step: k_lpt_order, k_gate_slots, k_compile_dd, k_run (schedule 1; the launch list in
         # profiles/), or k_lpt_order, k_compile and two k_run (schedule 0)
         "gpu_launches": 4 * a.steps,
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "peak_kind": f"{peaks_kind} bf16 sustained",
                      "traffic": (tr["bytes_per_flop"] * per_launch) if tr else None,
-                     "traffic_source": "profiles/k_run_traffic.json: DRAM bytes per algorithmic flop of a "
-                                       "full-size launch (ncu), times this launch's flops" if tr else None,
+                     "traffic_source": tr.get("source") if tr else None,
                      "algorithmic_flops_per_launch": per_launch,
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "launch_ms_mean": launch_s * 1e3,
                      "simt_fp32": {"peak_tflops_nominal": simt_peak, "frac": achieved / simt_peak},
-                     "kernel": "k_run (theta build + Jacobi SVD + truncation + measurement, one CTA per trajectory)"},
+                     "kernel": "k_run (theta build + Jacobi SVD + truncation + measurement, one CTA per work item)"},
         "clocks": r["clocks"],
-        "work": {"bond_ops_per_step": r["stats"]["bond_ops"] / a.steps,
+        "work": {"batch_per_gpu": r["B"], "gpu": r["gpu"],
+                 "bond_ops_per_step": r["stats"]["bond_ops"] / a.steps,
                  "jacobi_sweeps_per_op": r["stats"]["sweeps"] / max(1.0, r["stats"]["bond_ops"]),
                  "meas_per_step": r["stats"]["meas"] / a.steps, "step_ms": r["step_ms"],
+                 "host_step_s": r["host_step_s"], "untimed_layer_ms": r["untimed_ms"],
                  "schedule": ("one launch per layer, sweeps pushed as gates finish" if a.schedule == 1
                               else "two launches per layer (gates, then sweeps)"),
                  "launch_ms (gate+sweep launch | gate launch, sweep launch)": r["split"],
@@ -838,19 +835,21 @@ def main():
                                           r["stats"]["nonconv_c_direct"]],
                  "device_status": r["status"], "middle_bond_dims": [int(d[a.n // 2 - 1]) for d in r["dims"]]},
     }
-    if rank == 0 and world == 1 and not a.no_plain:
+    if rank == 0 and world == 1 and r["plain_states"]:
         import __graft_entry__ as ge
-        pl = run_plain(a, ge.load_package())
+        pl = run_plain(a, ge.load_package(), r["plain_states"])
         out["plain_gpu"] = pl
         out["batched_over_plain"] = r["value"] / pl["value"]
     if rank == 0 and world == 1 and a.serve_seconds > 0:
         import __graft_entry__ as ge
         out["serving"] = run_serving(a, ge.load_package())
-    if rank == 0 and world == 1 and not a.no_cpu:
-        t = a.prefill + a.warmup
-        layers = [r["layer_inputs"](t)[i] for i in range(min(r["B"], 16))]
-        cb = cpu_baseline(a.n, a.chi, a.cutoff, layers, a.cpu_seconds)
+    if cpu_async is not None:
+        res = cpu_async.get()
+        cpu_pool.close()
+        cpu_pool.join()
+        cb = summarize_reference(res, t_first, a.cpu_seconds)
         out["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        out["cpu_baseline"]["seconds_per_traj_layer_per_core"] = cb["seconds_per_traj_layer_per_core"]
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

@@ -216,5 +216,12 @@ class Batch:
         s = L.check(self._lib.tn_batch_last_launch_ms(self._h, C.byref(g), C.byref(w)), "last_launch_ms")
         return None if s == L.TN_NONE else (g.value, w.value)
 
+    def last_step_device_ms(self):
+        """Device time of the last host-input step from the end of its input
+        copy to the start of its output copy (every kernel of the layer)."""
+        ms = C.c_float()
+        s = L.check(self._lib.tn_batch_last_step_device_ms(self._h, C.byref(ms)), "last_step_device_ms")
+        return None if s == L.TN_NONE else ms.value
+
     def synchronize(self):
         L.check(self._lib.tn_batch_synchronize(self._h), "synchronize")
