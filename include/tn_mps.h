@@ -339,6 +339,15 @@ int tn_batch_last_launch_ms(tn_batch *b, float *gate_ms, float *sweep_ms);
  * output copy: every kernel of the layer, with its inputs resident in HBM.
  * TN_NONE before the first such step. */
 int tn_batch_last_step_device_ms(tn_batch *b, float *ms);
+/* Failure detection of the one-launch schedule (no counterpart in the
+ * reference).  A CTA that has claimed a sweep slot waits for the item to be
+ * pushed at most wait_ns nanoseconds (0 = the default, 120 s); past it, the
+ * CTA sets ST_QUEUE_WAIT (bit 16 of tn_batch_device_status) and moves on, so
+ * the launch always ends.  phantom_sweeps adds sweep slots that no work item
+ * ever fills (capped by the step buffers' trajectory capacity), which makes
+ * the wait run out on purpose: a test of the limit and of the error report.
+ * Both settings hold for later steps until changed. */
+int tn_batch_set_queue_wait(tn_batch *b, uint64_t wait_ns, uint32_t phantom_sweeps);
 /* Stream the batch launches on (a cudaStream_t), for callers that time with
  * CUDA events. */
 int tn_batch_stream(tn_batch *b, void **stream);

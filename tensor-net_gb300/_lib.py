@@ -91,6 +91,7 @@ SIGNATURES = {
     "tn_batch_stream": (C.c_int, [vp, P(vp)]),
     "tn_batch_last_launch_ms": (C.c_int, [vp, P(C.c_float), P(C.c_float)]),
     "tn_batch_last_step_device_ms": (C.c_int, [vp, P(C.c_float)]),
+    "tn_batch_set_queue_wait": (C.c_int, [vp, C.c_uint64, C.c_uint32]),
     "tn_batch_set_tuning": (C.c_int, [vp, i32, i32]),
     "tn_server_create": (C.c_int, [u64, u32, i32, u32, u32, P(vp)]),
     "tn_batch_set_schedule": (C.c_int, [vp, i32]),

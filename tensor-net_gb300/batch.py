@@ -216,6 +216,11 @@ class Batch:
         s = L.check(self._lib.tn_batch_last_launch_ms(self._h, C.byref(g), C.byref(w)), "last_launch_ms")
         return None if s == L.TN_NONE else (g.value, w.value)
 
+    def set_queue_wait(self, wait_ns: int = 0, phantom_sweeps: int = 0):
+        """Limit of a CTA's wait for a pushed sweep item (0: 120 s) and sweep
+        slots that no item fills (to make that wait run out in a test)."""
+        L.check(self._lib.tn_batch_set_queue_wait(self._h, int(wait_ns), int(phantom_sweeps)), "set_queue_wait")
+
     def last_step_device_ms(self):
         """Device time of the last host-input step from the end of its input
         copy to the start of its output copy (every kernel of the layer)."""

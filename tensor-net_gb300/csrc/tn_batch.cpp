@@ -98,6 +98,10 @@ struct tn_batch {
   // device interval of the last host-input step between its input copy and
   // its output copy (every kernel of the step, inputs resident in HBM)
   cudaEvent_t ev_step[2] = {nullptr, nullptr};
+  // limit of a CTA's wait for a pushed sweep item (0: kQueueWaitNs), and
+  // sweep slots that no item ever fills (a test of that limit)
+  unsigned long long queue_wait_ns = 0;
+  uint32_t phantom_sweeps = 0;
   bool ev_step_recorded = false;
   uint32_t pending_nt = 0, pending_nm = 0;
   bool async_step = false;        // engine mode: tn_batch_step returns before the outputs arrive
@@ -283,7 +287,8 @@ int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P0, bool timed = true)
     // trajectory's sweep program as soon as its last gate item has finished.
     CKB(cudaMemsetAsync(b->dcounter, 0, 4 * sizeof(int), b->st));
     CKB(cudaMemsetAsync(b->dcounter + 8, 0, 3 * sizeof(int), b->st));  // push tail, queue error, sweep head
-    CKB(cudaMemsetAsync(b->ddyn, 0, sizeof(Item) * nt, b->st));
+    const uint32_t phantom = std::min<uint32_t>(b->phantom_sweeps, b->step_nt - std::min(b->step_nt, nt));
+    CKB(cudaMemsetAsync(b->ddyn, 0, sizeof(Item) * (nt + phantom), b->st));
     CKB(launch_compile_dd(b->dtraj, P.list, int(nt), P.order, P.goff, P.gks, P.moff, P.mks, P.posts, b->pcap,
                           b->dprog, b->ditems, b->dgprog, b->dgitems, b->gcap, b->dcounter + 3, b->dgstart,
                           b->dscratch, b->drem, b->ddyn, b->dcounter + 8, b->st));
@@ -298,7 +303,8 @@ int launch_step(tn_batch *b, uint32_t nt, const StepPtrs &P0, bool timed = true)
     la.dyn = b->ddyn;
     la.dyn_tail = b->dcounter + 8;
     la.dyn_head = b->dcounter + 10;
-    la.nsweeps = int(nt);
+    la.nsweeps = int(nt + phantom);
+    la.queue_wait_ns = b->queue_wait_ns;
     if (timed) CKB(cudaEventRecord(b->ev[0], b->st));
     CKB(launch_run(b->prec, la, gmax, b->sortP, b->maxcap, b->st));
     if (timed) {
@@ -870,6 +876,15 @@ int tn_batch_last_launch_ms(tn_batch *b, float *gate_ms, float *sweep_ms) {
   if (!b->ev_one_launch) CKB(cudaEventElapsedTime(&w, b->ev[1], b->ev[2]));
   if (gate_ms) *gate_ms = g;
   if (sweep_ms) *sweep_ms = w;
+  return TN_OK;
+}
+
+int tn_batch_set_queue_wait(tn_batch *b, uint64_t wait_ns, uint32_t phantom_sweeps) {
+  if (!b) return TN_ERR_INVALID_ARG;
+  b->queue_wait_ns = wait_ns;
+  b->phantom_sweeps = phantom_sweeps;
+  for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);  // captured with the old settings
+  b->graphs.clear();
   return TN_OK;
 }
 

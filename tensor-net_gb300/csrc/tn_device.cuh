@@ -19,6 +19,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "tn_dd.cuh"
 #include "tn_internal.h"
 #include "tn_tc.cuh"
@@ -694,6 +696,106 @@ __device__ void gram_stream(const cpx<T> *__restrict__ A, int ell, const int *co
   __syncthreads();
 }
 
+// Row p and column q (p <= q) of entry e of the upper triangle of a W x W
+// matrix, row by row.
+template <int W>
+__device__ __forceinline__ void upper_entry(int e, int &p, int &q) {
+  int r = 0, base = 0;
+  while (base + (W - r) <= e) {
+    base += W - r;
+    ++r;
+  }
+  p = r;
+  q = r + (e - base);
+}
+
+// Hermitian Gram of a double-float block, streamed: only the W (W + 1) / 2
+// entries with p <= q are summed (G_qp = conj G_pq).  Thread t < NT sums
+// upper entry t over every row; the remaining W (W + 1) / 2 - NT entries are
+// summed one per warp, each lane over every 32nd row, and reduced across the
+// warp at the end (double-float raw accumulators throughout).
+template <int NT, int W>
+__device__ void gram_stream_herm(const cpx<dd> *__restrict__ A, int ell, const int *cols, Smem<dd, W> &sm) {
+  constexpr int TP = W + 1, NE = W * (W + 1) / 2, NX = NE - NT;
+  static_assert(NX >= 0 && NX <= NT / 32, "one leftover entry per warp at most");
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int p0, q0, px = 0, qx = 0;
+  upper_entry<W>(threadIdx.x, p0, q0);
+  const bool extra = warp < NX;
+  if (extra) upper_entry<W>(NT + warp, px, qx);
+  cdacc acc = acc_zero<dd>(), accx = acc_zero<dd>();
+  for (int i0 = 0; i0 < ell; i0 += 32) {
+    __syncthreads();
+    load_block_chunk<dd, NT, W>(A, ell, cols, i0, sm.Ts);
+    __syncthreads();
+    const int rmax = min(32, ell - i0);
+    for (int r = 0; r < rmax; ++r) acc_jfma<dd>(acc, sm.Ts[r * TP + p0], sm.Ts[r * TP + q0]);
+    if (extra && lane < rmax) acc_jfma<dd>(accx, sm.Ts[lane * TP + px], sm.Ts[lane * TP + qx]);
+  }
+  cpx<dd> g = acc_fin<dd>(acc);
+  sm.G[p0 * TP + q0] = g;
+  if (p0 != q0) sm.G[q0 * TP + p0] = mkc<dd>(g.x, -g.y);
+  if (extra) {
+    cpx<dd> gx = acc_fin<dd>(accx);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      gx.x += shfl_xor(gx.x, o);
+      gx.y += shfl_xor(gx.y, o);
+    }
+    if (lane == 0) {
+      sm.G[px * TP + qx] = gx;
+      if (px != qx) sm.G[qx * TP + px] = mkc<dd>(gx.x, -gx.y);
+    }
+  }
+  __syncthreads();
+}
+
+// Float Gram of the leading halves of double-float vectors (the guided
+// sweeps of jacobi_svd<dd>): the 32-row chunks of the block's hi parts
+// staged as complex float in Ts, G (complex float, row pitch W + 1) written
+// over sm.G's area.  The hi parts carry each entry to float precision
+// relative to that entry (2^-24), the precision the float Gram needs.
+template <int NT, int W>
+__device__ void gram_stream_hi(const cpx<dd> *__restrict__ A, int ell, const int *cols, Smem<dd, W> &sm) {
+  constexpr int TP = W + 1;
+  constexpr int PER = (W * W + NT - 1) / NT;
+  cpx<float> *Ts = reinterpret_cast<cpx<float> *>(sm.Ts);
+  cpx<float> *G = reinterpret_cast<cpx<float> *>(sm.G);
+  cpx<float> acc[PER];
+#pragma unroll
+  for (int e = 0; e < PER; ++e) acc[e] = czero<float>();
+  for (int i0 = 0; i0 < ell; i0 += 32) {
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < 32 * W; idx += NT) {
+      const int r = idx & 31, q = idx >> 5;
+      cpx<float> v = czero<float>();
+      if (cols[q] >= 0 && i0 + r < ell) {
+        const cpx<dd> x = A[size_t(cols[q]) * ell + i0 + r];
+        v = mkc<float>(x.x.hi, x.y.hi);
+      }
+      Ts[r * TP + q] = v;
+    }
+    __syncthreads();
+    const int rmax = min(32, ell - i0);
+#pragma unroll
+    for (int e = 0; e < PER; ++e) {
+      const int o = threadIdx.x + e * NT;
+      if (o < W * W) {
+        const int pp = o / W, qq = o % W;
+        cpx<float> a = acc[e];
+        for (int r = 0; r < rmax; ++r) a = cjfma(Ts[r * TP + pp], Ts[r * TP + qq], a);
+        acc[e] = a;
+      }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < PER; ++e) {
+    const int o = threadIdx.x + e * NT;
+    if (o < W * W) G[(o / W) * (W + 1) + o % W] = acc[e];
+  }
+  __syncthreads();
+}
+
 // X (rows x W slice of a vector-contiguous matrix, vector length ld) <- X J
 template <typename T, int NT, int W>
 __device__ void update_stream(cpx<T> *__restrict__ X, int ld, int rows, const int *cols,
@@ -1048,6 +1150,71 @@ __device__ const cpx<T> *jacobi_gram(Smem<T, W> &sm, const int *cols, T tol, T t
   return J;
 }
 
+// The inner sweep of a guided step (jacobi_svd<dd>): the rotations are
+// chosen on the float Gram in sm.G's area exactly as jacobi_gram chooses
+// them, but each is rebuilt in double-float as an exactly unitary rotation
+// -- c = 1 / sqrt(1 + t^2), s = t c from the float tangent t = s / c, the
+// phase e normalised to modulus 1 -- and only those rebuilt rotations are
+// accumulated into J (double-float).  The angles are float accurate, which
+// is all an early sweep needs; J stays unitary to the double-float rounding,
+// so applying it to the double-float vectors changes no singular value
+// beyond that rounding.
+template <int NT, int W>
+__device__ const cpx<dd> *jacobi_gram_guided(Smem<dd, W> &sm, float tol, float tiny2, int mode, int inner) {
+  constexpr int H = W / 2, GP = W + 1;
+  static_assert(W == 32 && NT / 32 == H, "one warp per rotation pair");
+  cpx<float> *G = reinterpret_cast<cpx<float> *>(sm.G);
+  cpx<dd> *J = sm.J;
+  const int lane = threadIdx.x & 31, t = threadIdx.x >> 5;
+  for (int idx = threadIdx.x; idx < W * W; idx += NT) {
+    const int p = idx / W, q = idx % W;
+    J[p * GP + q] = (p == q) ? mkc<dd>(dd(1.f, 0.f), dd(0.f, 0.f)) : czero<dd>();
+  }
+  const int rounds = mode == 0 ? W - 1 : (mode == 1 ? H : H - 1);
+  for (int r = 0; r < rounds * inner; ++r) {
+    int p, q;
+    if (mode == 0) {
+      rr_pair<W>(r, t, p, q);
+    } else if (mode == 1) {
+      p = t;
+      q = H + (t + r) % H;
+    } else {
+      const int h = t / (H / 2), tt = t % (H / 2);
+      rr_pair<H>(r, tt, p, q);
+      p += h * H;
+      q += h * H;
+    }
+    float c = 1.f, sn = 0.f;
+    cpx<float> e = mkc<float>(1.f, 0.f);
+    const bool rot = jacobi_rotation<float>(G[p * GP + p].x, G[q * GP + q].x, G[p * GP + q], tol, tiny2, c, sn, e);
+    __syncwarp();
+    if (rot) {
+      const cpx<float> gp = G[p * GP + lane], gq = G[q * GP + lane];
+      const cpx<float> egq = cmul(mkc<float>(e.x, -e.y), gq);
+      G[p * GP + lane] = mkc<float>(c * gp.x - sn * egq.x, c * gp.y - sn * egq.y);
+      G[q * GP + lane] = mkc<float>(sn * gp.x + c * egq.x, sn * gp.y + c * egq.y);
+    }
+    __syncthreads();
+    if (rot) {
+      const int i = lane;
+      const cpx<float> gp = G[i * GP + p], gq = cmul(e, G[i * GP + q]);
+      G[i * GP + p] = mkc<float>(c * gp.x - sn * gq.x, c * gp.y - sn * gq.y);
+      G[i * GP + q] = mkc<float>(sn * gp.x + c * gq.x, sn * gp.y + c * gq.y);
+      // the same rotation, exactly unitary in double-float
+      const dd td = dd(sn) / dd(c);
+      const dd cd = dd(1.f) / sqrt(dd(1.f) + td * td), sd = td * cd;
+      const dd ex = dd(e.x), ey = dd(e.y);
+      const dd er = sqrt(ex * ex + ey * ey);
+      const cpx<dd> ed = mkc<dd>(ex / er, ey / er);
+      const cpx<dd> jp = J[i * GP + p], jq = cmul(ed, J[i * GP + q]);
+      J[i * GP + p] = mkc<dd>(cd * jp.x - sd * jq.x, cd * jp.y - sd * jq.y);
+      J[i * GP + q] = mkc<dd>(sd * jp.x + cd * jq.x, sd * jp.y + cd * jq.y);
+    }
+    __syncthreads();
+  }
+  return J;
+}
+
 template <typename T, int NT, int W>
 __device__ void bitonic_desc(double *key, int *idx, int P);
 
@@ -1061,6 +1228,12 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
   // the threshold sits a factor 4 above it so that converged pairs are not
   // rotated again on noise alone.
   const T tol = T(4) * sqrt(T(ell)) * Eps<T>::v;
+  // Double-float: the sweeps start guided (float Gram of the hi parts, float
+  // rotation angles, double-float rotations and update) until a sweep finds
+  // no pair above the float threshold; the last sweeps run in double-float.
+  constexpr bool kDD = std::is_same<T, dd>::value;
+  bool guided = kDD;
+  const float tol_f = 4.f * sqrtf(float(ell)) * Eps<float>::v;
   // Columns with |a|^2 <= eps^2 ||A||_F^2 are rounding noise: rotating them
   // changes nothing above rounding and their relative off-diagonals never
   // settle, so they are neither rotated nor counted for convergence.
@@ -1071,6 +1244,7 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
   }
   fro = block_sum<NT>(fro, sm.red);
   const T tiny2 = T(fro * sweep_floor<T>(ell) * sweep_floor<T>(ell));
+  const float tiny2_f = float(fro * double(Eps<float>::v) * double(Eps<float>::v));
   const int nblk = (c + B - 1) / B;
   int *cols = sm.ired + 128;  // W ints (ired[0..128) is reduction scratch)
   // Column norms^2, kept current from the rotated Gram diagonals; each sweep
@@ -1202,7 +1376,14 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
           gram_stream<T, NT, W>(A, ell, cols, sm);
         }
       } else {
-        gram_stream<T, NT, W>(A, ell, cols, sm);
+        if constexpr (kDD) {
+          if (guided)
+            gram_stream_hi<NT, W>(A, ell, cols, sm);
+          else
+            gram_stream_herm<NT, W>(A, ell, cols, sm);
+        } else {
+          gram_stream<T, NT, W>(A, ell, cols, sm);
+        }
       }
       // Pairs above the threshold, split into pairs inside a half-block and
       // pairs across the two halves.  A step whose within-half pairs are all
@@ -1216,7 +1397,15 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
           const bool cross = (p < B) != (q < B);
           if (mode == 1 && !cross) continue;
           if (mode == 2 && cross) continue;
-          if (pair_active<T>(sm.G[p * (W + 1) + p].x, sm.G[q * (W + 1) + q].x, sm.G[p * (W + 1) + q], tol, tiny2)) {
+          bool act;
+          if (kDD && guided) {
+            const cpx<float> *Gf = reinterpret_cast<const cpx<float> *>(sm.G);
+            act = pair_active<float>(Gf[p * (W + 1) + p].x, Gf[q * (W + 1) + q].x, Gf[p * (W + 1) + q], tol_f,
+                                     tiny2_f);
+          } else {
+            act = pair_active<T>(sm.G[p * (W + 1) + p].x, sm.G[q * (W + 1) + q].x, sm.G[p * (W + 1) + q], tol, tiny2);
+          }
+          if (act) {
             if (cross)
               needC = 1;
             else
@@ -1233,7 +1422,13 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
       cyc[3] += 1;
       if (need) {
         rotated = 1;
-        const cpx<T> *Jm = jacobi_gram<T, NT, W>(sm, cols, tol, tiny2, mode, inner);
+        const cpx<T> *Jm;
+        if constexpr (kDD) {
+          Jm = guided ? jacobi_gram_guided<NT, W>(sm, tol_f, tiny2_f, mode, inner)
+                      : jacobi_gram<T, NT, W>(sm, cols, tol, tiny2, mode, inner);
+        } else {
+          Jm = jacobi_gram<T, NT, W>(sm, cols, tol, tiny2, mode, inner);
+        }
         long long t2 = clock64();
         cyc[1] += t2 - t1;
         t1 = t2;
@@ -1247,12 +1442,20 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
         } else {
           update_stream<T, NT, W>(A, ell, ell, cols, Jm, sm);
         }
-        if (nblk > 2 && threadIdx.x < W && cols[threadIdx.x] >= 0)
-          nrm[cols[threadIdx.x]] = double(sm.G[threadIdx.x * (W + 2)].x);
+        if (nblk > 2 && threadIdx.x < W && cols[threadIdx.x] >= 0) {
+          if (kDD && guided)
+            nrm[cols[threadIdx.x]] = double(reinterpret_cast<const cpx<float> *>(sm.G)[threadIdx.x * (W + 2)].x);
+          else
+            nrm[cols[threadIdx.x]] = double(sm.G[threadIdx.x * (W + 2)].x);
+        }
         cyc[2] += clock64() - t1;
       }
     }
     if (!rotated) {
+      if (guided) {  // float-converged: the remaining sweeps in double-float
+        guided = false;
+        continue;
+      }
       flush();
       return sweep + 1;
     }

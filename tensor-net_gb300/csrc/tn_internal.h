@@ -105,6 +105,7 @@ struct LaunchArgs {
   int *dyn_head;          // sweep slots claimed; zeroed before the launch
   int nsweeps;
   int *qerr;              // set to 1 when a queue wait ran past its time limit
+  unsigned long long queue_wait_ns;  // limit of one such wait (0: kQueueWaitNs)
 };
 
 // Default Jacobi block scheme (see jacobi_svd): all pairs of each block pair,

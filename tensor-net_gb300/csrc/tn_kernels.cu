@@ -105,9 +105,10 @@ __global__ void __launch_bounds__(NT, 1) k_run(LaunchArgs la, int sortP, int ws_
       if (slot_i >= 0) {
         Item *slot = la.dyn + slot_i;
         const unsigned long long t0 = global_ns();
+        const unsigned long long limit = la.queue_wait_ns ? la.queue_wait_ns : kQueueWaitNs;
         kind = 2;
         while (load_acquire(&slot->aux) == 0) {
-          if (global_ns() - t0 > kQueueWaitNs) {
+          if (global_ns() - t0 > limit) {
             atomicExch(la.qerr, 1);
             kind = 3;
             break;

@@ -72,3 +72,30 @@ def test_coevolution_from_cbor_circuit_files(pkg, tmp_path):
     np.testing.assert_array_equal(a["outcomes"], b["outcomes"])
     np.testing.assert_array_equal(a["probs"], b["probs"])
     assert a["device_status"] == (0, 0)
+
+
+@pytest.mark.parametrize("prec", ["f64", "df"])
+def test_cbor_circuit_files_through_the_gpu_match_the_oracle(pkg, ref, tmp_path, prec):
+    """A seeded Haar brickwork circuit written to the reference's CBOR
+    formats (Vec<Vec<Uni>> and Vec<Vec<Meas>>, circuit.rs:479-517), read back
+    and run through the GPU single-state API, against the FP64 oracle fed the
+    original arrays: outcomes, probabilities and per-layer entropies."""
+    from tensor_net_gb300 import circuits
+    from tensor_net_gb300.gates import Meas
+    n, chi, depth, p, seed = 10, 16, 8, 0.25, 33
+    layers = pkg.gen_trajectory(seed, 0, n, depth, p)
+    circuits.save_uni_layers(tmp_path / "unis.cbor",
+                             [circuits.uni_layer_from_arrays(gk, g) for (gk, g, _, _) in layers])
+    circuits.save_meas_layers(tmp_path / "meas.cbor", [[Meas.rand(int(k)) for k in mk] for (_, _, mk, _) in layers])
+    unis = circuits.load_uni_layers(tmp_path / "unis.cbor")
+    meas = circuits.load_meas_layers(tmp_path / "meas.cbor")
+    assert len(unis) == len(meas) == depth
+    g = pkg.MPS.new_qubits(n, pkg.Trunc.both(chi, 1e-12), prec)
+    r = ref.MPS(n, ref.Trunc.both(chi, 1e-12))
+    for (gk, gs, mk, us), ul, ml in zip(layers, unis, meas):
+        outs, probs = g.apply_bilayer_ops(ul, ml, us)
+        rec = ref.apply_bilayer(r, gk, gs, mk, us)
+        assert [(m.k, m.outcome) for m in outs] == [(k, o) for (k, o, _) in rec]
+        np.testing.assert_allclose([q for (_, q) in probs], [q for (_, _, q) in rec], atol=1e-9)
+        assert abs(g.entropy_vn(n // 2 - 1) - r.entropy_vn(n // 2 - 1)) < 1e-9
+    assert g.device_status() == 0

@@ -47,3 +47,29 @@ def test_non_finite_inputs_are_refused(pkg):
         assert e.value.status == -6
     recs, ents = b.step([0, 1], [(gk, g, mk, us)] * 2)  # a good step still runs
     assert recs[0] == recs[1] and b.device_status() == 0
+
+
+def test_queue_wait_limit_runs_out_and_is_reported(pkg):
+    """A CTA's wait for a pushed sweep item is bounded: with one sweep slot
+    that no work item ever fills and a 5 ms limit, the launch still ends,
+    the batch reports ST_QUEUE_WAIT (bit 16), the real trajectories' results
+    are those of an ordinary batch, and the next ordinary step is clean."""
+    ns = [10, 12, 9]
+    truncs = [pkg.Trunc.both(16, 1e-12)] * 3
+    test, ref = pkg.Batch(ns, truncs, "mixed"), pkg.Batch(ns, truncs, "mixed")
+    layers = [pkg.gen_layer(41, i, 0, n, 0.2) for i, n in enumerate(ns)]
+    for b in (test, ref):
+        b.step([0, 1, 2], layers)  # sizes the step buffers for three trajectories
+    assert test.device_status() == 0
+    test.set_queue_wait(5_000_000, 1)  # 5 ms, one phantom sweep slot
+    layers = [pkg.gen_layer(41, i, 1, n, 0.2) for i, n in enumerate(ns)]
+    r_t, e_t = test.step([0, 1], layers[:2])
+    r_r, e_r = ref.step([0, 1], layers[:2])
+    assert test.device_status() & 16
+    assert r_t == r_r and list(e_t) == list(e_r)
+    test.set_queue_wait(0, 0)
+    layers = [pkg.gen_layer(41, i, 2, n, 0.2) for i, n in enumerate(ns)]
+    r_t, e_t = test.step([0, 1, 2], layers)
+    r_r, e_r = ref.step([0, 1, 2], layers)
+    assert test.device_status() == 0 and ref.device_status() == 0
+    assert r_t == r_r and list(e_t) == list(e_r)

@@ -333,3 +333,22 @@ def test_autotuner_tries_every_candidate_and_keeps_the_best(pkg):
     cand = [(1, 3, 0), (1, 0, 0), (0, 3, 0), (1, 3, 1)][best]
     assert (st["schedule"], st["scheme"], st["theta_simt"]) == cand
     assert tuned.device_status() == 0
+
+
+@pytest.mark.parametrize("prec", ["f64", "df", "mixed"])
+def test_entropy_ry_schmidt_matches_oracle(pkg, ref, prec):
+    """entropy_ry_schmidt (mps.rs:1268-1282): the Renyi entropy of the Schmidt
+    values of every bond for a in {0.5, 1, 2, 3} (a = 1 is entropy_vn) after
+    a seeded trajectory, and None off the chain."""
+    n, chi = 9, 16
+    g, r = _pair(pkg, ref, n, ("both", (chi, 1e-12)), prec)
+    for (gk, gs, mk, us) in pkg.gen_trajectory(5, 0, n, 6, 0.2):
+        g.apply_bilayer(gk, gs, mk, us)
+        ref.apply_bilayer(r, gk, gs, mk, us)
+    for b in range(n - 1):
+        for a in (0.5, 1.0, 2.0, 3.0):
+            ea, er = g.entropy_ry_schmidt(a, b), r.entropy_ry_schmidt(a, b)
+            assert abs(ea - er) < TOL[prec], (b, a, ea, er)
+        assert g.entropy_ry_schmidt(1.0, b) == g.entropy_vn(b)
+    assert g.entropy_ry_schmidt(2.0, n - 1) is None and r.entropy_ry_schmidt(2.0, n - 1) is None
+    assert g.device_status() == 0
