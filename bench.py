@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--batch", type=int, default=512, help="trajectories per GPU")
+    ap.add_argument("--batch", type=int, default=152, help="trajectories per GPU")
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--chi", type=int, default=256)
     ap.add_argument("--cutoff", type=float, default=1e-10)
@@ -78,6 +78,8 @@ def parse():
     ap.add_argument("--serve-active-per-cta", type=int, default=2,
                     help="resident requests per class = this x the class's CTAs (0 = every slot)")
     ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-sustained-rate", type=float, default=1.0)
+    ap.add_argument("--serve-sustained-seconds", type=float, default=30.0)
     ap.add_argument("--serve-hbm-gb", type=int, default=96)
     ap.add_argument("--serve-slots", type=int, default=1024)
     return ap.parse_args()
@@ -399,50 +401,84 @@ def run_plain(a, pkg, states):
                    f"[{t_lo}, {t_lo + nl}), host-timed"}
 
 
-def run_serving(a, pkg):
-    """Poisson serving window of the serving workload (arrivals at
-    --serve-rate/s, n log-uniform in [16, 128], chi_max in {64..512}, p in
-    [0.02, 0.3], depth in [2n, 4n]); latency = completion - arrival."""
-    reqs = pkg.poisson_requests(a.serve_rate, a.serve_seconds, a.seed)
-    srv = pkg.Server(int(a.serve_hbm_gb) << 30, max_slots=a.serve_slots, precision=a.prec, max_chi=512, max_n=128)
+def _censored_pct(values, q):
+    """q-th percentile of latencies where some are lower bounds (requests still
+    queued or running when the window closed): (value, censored)."""
+    if not values:
+        return None, False
+    v = sorted(values, key=lambda x: x[0])
+    x, cens = v[min(len(v) - 1, int(math.ceil(q / 100.0 * len(v))) - 1)]
+    return float(x), bool(cens)
+
+
+def _serve_window(pkg, a, reqs, duration, drain, max_chi, max_n, policy_caps=True):
+    srv = pkg.Server(int(a.serve_hbm_gb) << 30, max_slots=a.serve_slots, precision=a.prec, max_chi=max_chi,
+                     max_n=max_n)
     c0, c1 = srv.class_stats(0), srv.class_stats(1)
-    caps = (a.serve_active_per_cta * c0["ctas"], a.serve_active_per_cta * c1["ctas"]) if a.serve_active_per_cta else (0, 0)
+    caps = (a.serve_active_per_cta * c0["ctas"], a.serve_active_per_cta * c1["ctas"]) \
+        if (a.serve_active_per_cta and policy_caps) else (0, 0)
     srv.set_policy(a.serve_policy, caps)
     t0 = srv.now()
-    done, submitted = pkg.run_poisson(srv, reqs, a.serve_seconds, a.seed)
+    done, submitted = pkg.run_poisson(srv, reqs, duration, a.seed, drain=drain)
     wall = srv.now() - t0
     st = srv.stats()
     cls = [srv.class_stats(c) for c in (0, 1)]
     srv.close()
+    by_id = {d["id"]: d for d in done}
+    lat = []  # (latency or its lower bound, censored)
+    for i, r in enumerate(reqs[:submitted]):
+        d = by_id.get(i + 1)  # request ids are 1 + submission index
+        lat.append((d["latency_s"], False) if d else (max(0.0, wall - r["t"]), True))
 
-    def pct(lat, q):
-        lat = sorted(lat)
-        if not lat:
-            return None
-        return float(lat[min(len(lat) - 1, int(math.ceil(q / 100.0 * len(lat))) - 1)])
-    lat = [d["latency_s"] for d in done]
-    per_class = []
+    def summary(idx):
+        ls = [lat[i] for i in idx]
+        p50, c50 = _censored_pct(ls, 50)
+        p99, c99 = _censored_pct(ls, 99)
+        fin = sorted(x for x, c in ls if not c)
+        return {"submitted": len(ls), "completed": len(fin),
+                "p50_latency_s": p50, "p50_censored": c50, "p99_latency_s": p99, "p99_censored": c99,
+                "p50_latency_completed_s": fin[len(fin) // 2] if fin else None}
+    out = {"wall_s": wall, "traj_layers_per_s": st["layers"] / wall if wall > 0 else None,
+           "admitted": int(st["admitted"]), "active_at_end": int(st["active"]), "pending_at_end": int(st["pending"]),
+           "all": summary(range(len(lat))), "max_active_per_class": list(caps), "classes": []}
     for c, cs in enumerate(cls):
         if cs["cap_max"] == 0:
             continue
         lo = cls[c - 1]["cap_max"] if c > 0 else 0
-        # request ids are 1 + submission index
-        lc = [d["latency_s"] for d in done if lo < min(reqs[d["id"] - 1]["chi"], 1 << (reqs[d["id"] - 1]["n"] // 2))
-              <= cs["cap_max"]]
-        sub = sum(1 for r in reqs[:submitted] if lo < min(r["chi"], 1 << (r["n"] // 2)) <= cs["cap_max"])
-        per_class.append({"bond_cap_max": cs["cap_max"], "ctas": cs["ctas"], "submitted": sub,
-                          "completed": len(lc), "p50_latency_s": pct(lc, 50), "p99_latency_s": pct(lc, 99),
-                          "traj_layers_per_s": cs["layers"] / wall if wall > 0 else None,
-                          "launches": int(cs["launches"]), "active_at_end": cs["active"],
-                          "pending_at_end": cs["pending"]})
-    return {"rate_per_s": a.serve_rate, "window_s": a.serve_seconds, "wall_s": wall, "submitted": submitted,
-            "policy": a.serve_policy, "max_active_per_class": list(caps),
-            "admitted": int(st["admitted"]), "completed": len(done), "active_at_end": int(st["active"]),
-            "pending_at_end": int(st["pending"]), "p50_latency_s": pct(lat, 50), "p99_latency_s": pct(lat, 99),
-            "traj_layers_per_s": st["layers"] / wall if wall > 0 else None, "ticks": int(st["ticks"]),
-            "classes": per_class,
-            "note": "latency percentiles over the requests completed inside the window (the offered load "
-                    "exceeds capacity: most heavy requests are still running or queued when it closes)"}
+        idx = [i for i, r in enumerate(reqs[:submitted]) if lo < min(r["chi"], 1 << (r["n"] // 2)) <= cs["cap_max"]]
+        out["classes"].append(dict(summary(idx), bond_cap_max=cs["cap_max"], ctas=cs["ctas"],
+                                   traj_layers_per_s=cs["layers"] / wall if wall > 0 else None,
+                                   launches=int(cs["launches"])))
+    return out
+
+
+def run_serving(a, pkg):
+    """Two serving windows through the continuous-batching server:
+    1. the serving workload as specified (Poisson arrivals at --serve-rate/s,
+       n log-uniform in [16, 128], chi_max in {64..512}, p in [0.02, 0.3],
+       depth in [2n, 4n]) for --serve-seconds: the offered load is far above
+       one GPU's capacity, so most requests are still queued or running when
+       the window closes; latency percentiles are over every submitted
+       request, unfinished ones counted at their time in the system so far
+       (a lower bound, flagged "censored");
+    2. a load the server sustains: light requests (n in [16, 32], chi_max in
+       {32, 64}) at --serve-sustained-rate/s for --serve-sustained-seconds,
+       then drained, so every submitted request completes and the
+       percentiles are exact."""
+    heavy = pkg.poisson_requests(a.serve_rate, a.serve_seconds, a.seed)
+    w1 = _serve_window(pkg, a, heavy, a.serve_seconds, False, 512, 128)
+    w1.update(rate_per_s=a.serve_rate, window_s=a.serve_seconds,
+              mix="n log-uniform [16, 128], chi_max {64, 128, 256, 512}, p U[0.02, 0.3], depth U[2n, 4n]")
+    out = {"specified_load": w1}
+    if a.serve_sustained_seconds > 0:
+        light = pkg.poisson_requests(a.serve_sustained_rate, a.serve_sustained_seconds, a.seed + 1,
+                                     n_range=(16, 32), chis=(32, 64))
+        w2 = _serve_window(pkg, a, light, a.serve_sustained_seconds, True, 64, 32, policy_caps=False)
+        w2.update(rate_per_s=a.serve_sustained_rate, window_s=a.serve_sustained_seconds, drained=True,
+                  mix="n log-uniform [16, 32], chi_max {32, 64}, p U[0.02, 0.3], depth U[2n, 4n]")
+        out["sustained_load"] = w2
+    out["precision"] = a.prec
+    return out
 
 
 def _dev_view(torch, ptr, n, typestr):

@@ -660,10 +660,13 @@ int tn_batch_step_post(tn_batch *b, const uint32_t *trajs, uint32_t nt, const ui
   StepPtrs P = ptrs_of(L, reinterpret_cast<char *>(b->dstep));
   P.order = nullptr;  // ranked on the device from the current bond dimensions
   P.posts = posts ? reinterpret_cast<const int *>(reinterpret_cast<char *>(b->dstep) + L.posts) : nullptr;
-  CKB(cudaEventRecord(b->ev_step[0], b->st));
+  const bool step_ev = b->ev_step[0] && b->ev_step[1];  // (not created for the server's engines)
+  if (step_ev) CKB(cudaEventRecord(b->ev_step[0], b->st));
   if (int s = launch_step(b, nt, P)) return s;
-  CKB(cudaEventRecord(b->ev_step[1], b->st));
-  b->ev_step_recorded = true;
+  if (step_ev) {
+    CKB(cudaEventRecord(b->ev_step[1], b->st));
+    b->ev_step_recorded = true;
+  }
   const size_t out_bytes = L.total - L.out_off;
   CKB(cudaMemcpyAsync(hb + L.out_off, reinterpret_cast<char *>(b->dstep) + L.out_off, out_bytes,
                       cudaMemcpyDeviceToHost, b->st));
