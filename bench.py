@@ -47,14 +47,14 @@ UNIT = "traj-layers/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=152, help="trajectories per GPU")
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--chi", type=int, default=256)
     ap.add_argument("--cutoff", type=float, default=1e-10)
-    ap.add_argument("--prefill", type=int, default=10)
+    ap.add_argument("--prefill", type=int, default=4)
     ap.add_argument("--prec", default="df", choices=["df", "mixed", "f64"])
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)

@@ -16,6 +16,7 @@
 // local_renormalize (mps.rs:1147-1209).
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -277,8 +278,18 @@ struct SmemLayout {
   static constexpr int GP = W + 1;                // padded row pitch of G and J
   static constexpr size_t g_bytes = size_t(W) * GP * sizeof(cpx<T>);
   static constexpr size_t ts_bytes = size_t(32) * TP * sizeof(cpx<T>);
+  // double-float executor: staging of the block update on the tensor cores
+  // (OzUpdate): digit planes of a 128-row x 32 K-chunk of the block and of
+  // the 64 x 64 real rotation, plus per-row / per-column exponents
+  static constexpr int OZ_DIGITS = 8, OZ_MT = 128, OZ_KC = 32, OZ_N = 64;
+  static constexpr size_t oz_a_plane = size_t(OZ_MT) * OZ_KC * 2, oz_b_plane = size_t(OZ_N) * OZ_N * 2;
+  static constexpr size_t oz_bytes = std::is_same<T, dd>::value
+                                         ? OZ_DIGITS * (oz_a_plane + oz_b_plane) + 4 * OZ_MT * sizeof(float) +
+                                               (OZ_MT + OZ_N + W) * sizeof(int)
+                                         : 0;
   __host__ __device__ static size_t total(int P) {
-    return region0(P) + ab_bytes + 2 * g_bytes + ts_bytes + 128 * sizeof(double) + 256 * sizeof(int) + 512;
+    return region0(P) + ab_bytes + 2 * g_bytes + ts_bytes + 128 * sizeof(double) + 256 * sizeof(int) + 512 +
+           (oz_bytes ? oz_bytes + 1024 : 0);
   }
 };
 
@@ -294,6 +305,7 @@ struct Smem {
   uint32_t tmem = 0, phase = 0;
   bool tc = false;
   bool tc_fail = false;  // an MMA wait ran past its limit during the current bond op
+  unsigned char *oz = nullptr;  // double-float executor: tensor-core update staging (1024-byte aligned)
   __device__ Smem(unsigned char *base, int P) {
     using L = SmemLayout<T, W>;
     auto al = [](unsigned char *q) {
@@ -314,6 +326,8 @@ struct Smem {
     red = reinterpret_cast<double *>(p);
     p += 128 * sizeof(double);
     ired = reinterpret_cast<int *>(p);
+    p += 256 * sizeof(int);
+    if (L::oz_bytes) oz = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
   }
 };
 
@@ -826,6 +840,260 @@ __device__ void update_stream(cpx<T> *__restrict__ X, int ld, int rows, const in
       if (o < 32 * W) {
         int q = o >> 5, r = o & 31;
         if (cols[q] >= 0 && i0 + r < rows) X[size_t(cols[q]) * ld + i0 + r] = out[e];
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// -- double-float block update on the tensor cores -----------------------
+// x * 2^e (exact while the result is a normal float)
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }
+__device__ __forceinline__ float scale2f(float x, int e) {
+  while (e > 126) {
+    x = __fmul_rn(x, pow2f(126));
+    e -= 126;
+  }
+  while (e < -126) {
+    x = __fmul_rn(x, pow2f(-126));
+    e += 126;
+  }
+  return __fmul_rn(x, pow2f(e));
+}
+// Exponent e with |v| < 2^e for every |v| <= m (m the largest magnitude of a
+// row or column; 0 when m == 0).
+__device__ __forceinline__ int oz_exponent(float m) {
+  int e = 0;
+  if (m > 0.f) frexpf(m, &e);
+  return e;
+}
+// ND signed BITS-bit digits of the double-float x = hi + lo relative to 2^E
+// (|x| < 2^E): x = 2^E sum_j d_j 2^(-BITS (j + 1)) + r,
+// |r| <= 2^(E - BITS ND - 1); |d_0| <= 2^BITS, |d_j| <= 2^(BITS-1) after.
+// Each digit is an integer, exact in bf16 (BITS <= 7).
+template <int ND, int BITS = 7>
+__device__ __forceinline__ void oz_digits(float hi, float lo, int E, float (&d)[ND]) {
+  constexpr float R = float(1 << BITS);
+  float rh = scale2f(hi, BITS - E), rl = scale2f(lo, BITS - E);
+#pragma unroll
+  for (int j = 0; j < ND; ++j) {
+    d[j] = rintf(rh);
+    float s, e;
+    two_sum(__fsub_rn(rh, d[j]), rl, s, e);  // the remainder, exactly
+    rh = __fmul_rn(s, R);
+    rl = __fmul_rn(e, R);
+  }
+}
+// Element offset in a K-major, no-swizzle bf16 tile with KC values per row:
+// 8-row x 16-byte core matrices, 128 bytes apart along K, KC * 16 bytes
+// apart between 8-row groups.
+__device__ __forceinline__ uint32_t oz_elem(int r, int k, int KC) {
+  return uint32_t((r >> 3) * (KC * 8) + (k >> 3) * 64 + (r & 7) * 8 + (k & 7));
+}
+
+// A_b <- A_b J for the 32 double-float vectors cols[0..32) of A (vector
+// length ell) on the tensor cores, exact to the double-float level: an
+// Ozaki-style splitting.  The block is the real ell x 64 matrix X (re/im of
+// the 32 vectors interleaved) and J the real 64 x 64 embedding Y =
+// [[Jr, Ji], [-Ji, Jr]].  Each vector is first divided by a power of two
+// near its norm (2^-e_p, exact) and J's row p multiplied by the same 2^e_p,
+// so that the entries of one row of X are of comparable size.  Each row of X
+// (each column of Y) is then written relative to a power of two above its
+// largest entry as 8 signed 7-bit integer digits (bf16, exact); the digit
+// products of a pair (j, k) summed over the 64 K values stay below 2^21, and
+// the up to 8 pairs with j + k = L (weight 2^(-7 (L + 2))) accumulate,
+// exactly (below 2^22), in one FP32 tensor-memory accumulator per level
+// L = 0..7 (kind::f16 MMAs, 128 x 64 x 16; 8 x 64 = 512 columns).  The
+// levels are added from the largest in double-float and scaled back.
+// Dropped levels (j + k >= 8) weigh below 2^-49 of the scales.  Rows go in
+// tiles of 128, K in two chunks of 32 (the digit planes of a chunk:
+// 8 x 8 KB).  Returns false when an MMA wait ran past its limit.
+template <int NT, int W>
+__device__ bool update_ozaki(cpx<dd> *__restrict__ A, int ell, const int *cols, const cpx<dd> *__restrict__ Jm,
+                             const float *__restrict__ gdiag, Smem<dd, W> &sm) {
+  using L = SmemLayout<dd, W>;
+  constexpr int ND = L::OZ_DIGITS, MT = L::OZ_MT, KC = L::OZ_KC, NN = L::OZ_N, GP = W + 1;
+  static_assert(W == 32 && NT == 512 && NN == 2 * W && 2 * KC == NN, "Ozaki update layout");
+  constexpr uint32_t IDESC = tc::idesc_bf16(MT, NN);
+  __nv_bfloat16 *Ap = reinterpret_cast<__nv_bfloat16 *>(sm.oz);        // ND planes of MT x KC
+  __nv_bfloat16 *Bp = Ap + size_t(ND) * MT * KC;                        // ND planes of NN x NN (K = NN)
+  float *rmax = reinterpret_cast<float *>(Bp + size_t(ND) * NN * NN);   // 4 x MT partial row maxima
+  int *Erow = reinterpret_cast<int *>(rmax + 4 * MT);                   // MT
+  int *Fcol = Erow + MT;                                                // NN
+  float *vexp = reinterpret_cast<float *>(Fcol + NN);                   // W: 2^e_p near each vector's norm
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  bool ok = true;
+  if (tid < W) {
+    const float gd = gdiag[tid];  // the vector's squared norm (Gram diagonal before this step's rotations)
+    vexp[tid] = (cols[tid] >= 0 && gd > 0.f && isfinite(gd)) ? pow2f(oz_exponent(sqrtf(gd))) : 1.f;
+  }
+  __syncthreads();
+  // B: digit planes of diag(2^e_p) Y, column scale per output vector q
+  if (tid < W) {
+    float m = 0.f;
+    for (int pp = 0; pp < W; ++pp) {
+      const cpx<dd> j = Jm[pp * GP + tid];
+      const float sc = vexp[pp];
+      m = fmaxf(m, fmaxf(fabsf(j.x.hi), fabsf(j.y.hi)) * sc);
+    }
+    const int e = oz_exponent(m);
+    Fcol[2 * tid] = e;
+    Fcol[2 * tid + 1] = e;
+  }
+  __syncthreads();
+  for (int idx = tid; idx < NN * NN; idx += NT) {  // (c, k): output column c, K index k
+    const int c = idx >> 6, k = idx & 63;
+    const int q = c >> 1, b = c & 1, pp = k >> 1, a = k & 1;
+    const cpx<dd> j = Jm[pp * GP + q];
+    const dd y = (a == b) ? j.x : (a == 0 ? j.y : -j.y);
+    const float sc = vexp[pp];  // 2^e_p (exact scaling)
+    float d[ND];
+    oz_digits<ND>(__fmul_rn(y.hi, sc), __fmul_rn(y.lo, sc), Fcol[c], d);
+    const uint32_t off = oz_elem(c, k, NN);
+#pragma unroll
+    for (int jj = 0; jj < ND; ++jj) Bp[size_t(jj) * NN * NN + off] = __float2bfloat16_rn(d[jj]);
+  }
+  const int r = tid & (MT - 1), g = tid >> 7;  // row of the tile; vectors 8g .. 8g + 7
+  for (int i0 = 0; i0 < ell; i0 += MT) {
+    const int i = i0 + r;
+    cpx<dd> v[8];
+    float mx = 0.f;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int q = 8 * g + u;
+      cpx<dd> x = czero<dd>();
+      if (cols[q] >= 0 && i < ell) x = A[size_t(cols[q]) * ell + i];
+      const float inv = 1.f / vexp[q];  // 2^-e_q
+      x.x = dd(__fmul_rn(x.x.hi, inv), __fmul_rn(x.x.lo, inv));
+      x.y = dd(__fmul_rn(x.y.hi, inv), __fmul_rn(x.y.lo, inv));
+      v[u] = x;
+      mx = fmaxf(mx, fmaxf(fabsf(x.x.hi), fabsf(x.y.hi)));
+    }
+    rmax[g * MT + r] = mx;
+    __syncthreads();
+    if (tid < MT)
+      Erow[tid] = oz_exponent(fmaxf(fmaxf(rmax[tid], rmax[MT + tid]), fmaxf(rmax[2 * MT + tid], rmax[3 * MT + tid])));
+    __syncthreads();
+    const int E = Erow[r];
+    for (int chunk = 0; chunk < 2; ++chunk) {
+      if (chunk == 1) ok = wait_mma<dd, W>(sm) && ok;  // the planes of chunk 0 are free again
+      if ((g >> 1) == chunk) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+#pragma unroll
+          for (int a = 0; a < 2; ++a) {
+            const dd x = a ? v[u].y : v[u].x;
+            float d[ND];
+            oz_digits<ND>(x.hi, x.lo, E, d);
+            const uint32_t off = oz_elem(r, 16 * (g & 1) + 2 * u + a, KC);
+#pragma unroll
+            for (int jj = 0; jj < ND; ++jj) Ap[size_t(jj) * MT * KC + off] = __float2bfloat16_rn(d[jj]);
+          }
+        }
+      }
+      tc::fence_smem_to_async();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+        for (int lv = 0; lv < ND; ++lv) {
+          for (int ja = 0; ja <= lv; ++ja) {
+            const int jb = lv - ja;
+#pragma unroll
+            for (int ks = 0; ks < KC / 16; ++ks) {
+              const uint64_t ad = tc::smem_desc(reinterpret_cast<char *>(Ap + size_t(ja) * MT * KC) + ks * 256, 128,
+                                                KC * 16);
+              const uint64_t bd = tc::smem_desc(
+                  reinterpret_cast<char *>(Bp + size_t(jb) * NN * NN) + (chunk * (KC / 16) + ks) * 256, 128, NN * 16);
+              tc::mma_bf16(sm.tmem + uint32_t(64 * lv), ad, bd, IDESC, (chunk > 0 || ja > 0 || ks > 0) ? 1u : 0u);
+            }
+          }
+        }
+        tc::mma_commit(sm.bar);
+      }
+    }
+    ok = wait_mma<dd, W>(sm) && ok;
+    tc::fence_after_sync();
+    // epilogue: warp w reads rows 32 (w % 4) .. +31 and output columns 16 (w / 4) .. +15
+    const int row = 32 * (warp & 3) + lane, cq = warp >> 2;
+    dacc acc[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) acc[c].hi = acc[c].lo = 0.f;
+#pragma unroll 1
+    for (int lv = 0; lv < ND; ++lv) {
+      float t16[16];
+      tc::tmem_ld16(sm.tmem + (uint32_t(32 * (warp & 3)) << 16) + uint32_t(64 * lv + 16 * cq), t16);
+      const float wgt = pow2f(-7 * lv);
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        float s, e;
+        two_sum(acc[c].hi, __fmul_rn(t16[c], wgt), s, e);
+        acc[c].hi = s;
+        acc[c].lo = __fadd_rn(acc[c].lo, e);
+      }
+    }
+    const int ii = i0 + row;
+    if (ii < ell) {
+#pragma unroll
+      for (int qq = 0; qq < 8; ++qq) {
+        const int q = 8 * cq + qq;
+        if (cols[q] < 0) continue;
+        const int sh = Erow[row] + Fcol[2 * q] - 14;
+        const dd re = dd_norm(acc[2 * qq].hi, acc[2 * qq].lo), im = dd_norm(acc[2 * qq + 1].hi, acc[2 * qq + 1].lo);
+        A[size_t(cols[q]) * ell + ii] = mkc<dd>(dd(scale2f(re.hi, sh), scale2f(re.lo, sh)),
+                                              dd(scale2f(im.hi, sh), scale2f(im.lo, sh)));
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+  }
+  return ok;
+}
+
+// A_b <- A_b J for a double-float block when J is within kappa of the
+// identity (the finishing sweeps, after the guided ones: rotation angles of
+// the order of the float threshold and below): A_b + A_b (J - I), the
+// correction formed in float from the leading halves, which is accurate to
+// about 2^-24 kappa of the vectors, and added to the double-float values
+// exactly (TwoSum).  kappa <= 1e-6 keeps the correction's error below the
+// double-float threshold of the convergence test.
+template <int NT, int W>
+__device__ void update_near_identity(cpx<dd> *__restrict__ A, int ell, const int *cols, const cpx<dd> *__restrict__ Jm,
+                                     Smem<dd, W> &sm) {
+  constexpr int TP = W + 1, GP = W + 1;
+  cpx<float> *Ts = reinterpret_cast<cpx<float> *>(sm.Ts);       // 32 rows x W, hi parts
+  cpx<float> *K = reinterpret_cast<cpx<float> *>(sm.Ts) + 32 * TP;  // W x W: J - I in float
+  static_assert(sizeof(cpx<float>) * (32 * TP + W * GP) <= SmemLayout<dd, W>::ts_bytes, "fits Ts");
+  for (int idx = threadIdx.x; idx < W * W; idx += NT) {
+    const int pp = idx / W, q = idx % W;
+    cpx<dd> j = Jm[pp * GP + q];
+    if (pp == q) j.x = j.x - dd(1.f, 0.f);
+    K[pp * GP + q] = mkc<float>(float(j.x), float(j.y));
+  }
+  constexpr int PER = (32 * W + NT - 1) / NT;
+  for (int i0 = 0; i0 < ell; i0 += 32) {
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < 32 * W; idx += NT) {
+      const int r = idx & 31, q = idx >> 5;
+      cpx<float> v = czero<float>();
+      if (cols[q] >= 0 && i0 + r < ell) {
+        const cpx<dd> x = A[size_t(cols[q]) * ell + i0 + r];
+        v = mkc<float>(x.x.hi, x.y.hi);
+      }
+      Ts[r * TP + q] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < PER; ++e) {
+      const int o = threadIdx.x + e * NT;
+      if (o < 32 * W) {
+        const int q = o >> 5, r = o & 31;
+        if (cols[q] >= 0 && i0 + r < ell) {
+          cpx<float> c = czero<float>();
+          for (int pp = 0; pp < W; ++pp) c = cfma(Ts[r * TP + pp], K[pp * GP + q], c);
+          cpx<dd> &x = A[size_t(cols[q]) * ell + i0 + r];
+          const cpx<dd> y = x;
+          x = mkc<dd>(y.x + dd(c.x), y.y + dd(c.y));
+        }
       }
     }
   }
@@ -1422,6 +1690,15 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
       cyc[3] += 1;
       if (need) {
         rotated = 1;
+        // the vectors' squared norms before this step's rotations (scales of
+        // the tensor-core update)
+        float *gdiag = reinterpret_cast<float *>(sm.red);
+        if (kDD && threadIdx.x < W) {
+          if (guided)
+            gdiag[threadIdx.x] = reinterpret_cast<const cpx<float> *>(sm.G)[threadIdx.x * (W + 2)].x;
+          else
+            gdiag[threadIdx.x] = float(double(sm.G[threadIdx.x * (W + 2)].x));
+        }
         const cpx<T> *Jm;
         if constexpr (kDD) {
           Jm = guided ? jacobi_gram_guided<NT, W>(sm, tol_f, tiny2_f, mode, inner)
@@ -1440,7 +1717,32 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
             update_stream<T, NT, W>(A, ell, ell, cols, Jm, sm);
           }
         } else {
-          update_stream<T, NT, W>(A, ell, ell, cols, Jm, sm);
+          if constexpr (kDD) {
+            // finishing sweeps: how far J is from the identity (largest entry of J - I)
+            int near_id = 0;
+            if (!guided) {
+              float kmax = 0.f;
+              for (int idx = threadIdx.x; idx < W * W; idx += NT) {
+                const int pp = idx / W, q = idx % W;
+                cpx<dd> j = Jm[pp * (W + 1) + q];
+                if (pp == q) j.x = j.x - dd(1.f, 0.f);
+                kmax = fmaxf(kmax, fmaxf(fabsf(j.x.hi), fabsf(j.y.hi)));
+              }
+              near_id = __syncthreads_and(kmax <= 1e-6f);
+            }
+            // guided sweeps: the tensor-core update; finishing sweeps: the
+            // float correction when J is near the identity, else the exact
+            // double-float update (the finishing sweeps decide convergence at the
+            // double-float threshold, so they take no other rounding)
+            if (near_id)
+              update_near_identity<NT, W>(A, ell, cols, Jm, sm);
+            else if (sm.tc && guided)
+              update_ozaki<NT, W>(A, ell, cols, Jm, gdiag, sm);
+            else
+              update_stream<T, NT, W>(A, ell, ell, cols, Jm, sm);
+          } else {
+            update_stream<T, NT, W>(A, ell, ell, cols, Jm, sm);
+          }
         }
         if (nblk > 2 && threadIdx.x < W && cols[threadIdx.x] >= 0) {
           if (kDD && guided)

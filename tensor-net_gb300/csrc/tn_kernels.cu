@@ -53,9 +53,12 @@ __global__ void __launch_bounds__(NT, 1) k_run(LaunchArgs la, int sortP, int ws_
   Smem<T, W> sm(smem, sortP);
   Work<T> wk = make_work<T>(reinterpret_cast<unsigned char *>(la.ws) + size_t(blockIdx.x) * la.ws_stride, ws_cap);
   const bool dd = la.rem != nullptr;
-  constexpr uint32_t kTmemCols = 256;  // one 128 x 256 FP32 accumulator tile
-  if constexpr (sizeof(T) == 4) {
-    // the float executor owns kTmemCols tensor-memory columns for its whole
+  // float: one 128 x 256 FP32 accumulator tile (theta and recovery GEMMs);
+  // double-float: eight 128 x 64 level accumulators of the tensor-core update
+  constexpr bool kTC = sizeof(T) == 4 || std::is_same<T, ::tn::dd>::value;
+  constexpr uint32_t kTmemCols = sizeof(T) == 4 ? 256 : 512;
+  if constexpr (kTC) {
+    // the executor owns kTmemCols tensor-memory columns for its whole
     // life (one CTA per SM); released below on the kernel's only exit path
     if ((threadIdx.x >> 5) == 0) {
       tc::tmem_alloc(&s_tmem, kTmemCols);
@@ -136,7 +139,7 @@ __global__ void __launch_bounds__(NT, 1) k_run(LaunchArgs la, int sortP, int ws_
       }
     }
   }
-  if constexpr (sizeof(T) == 4) {
+  if constexpr (kTC) {
     tc::fence_before_sync();
     __syncthreads();
     if ((threadIdx.x >> 5) == 0) {
