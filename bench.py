@@ -50,14 +50,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--batch", type=int, default=152, help="trajectories per GPU")
+    ap.add_argument("--batch", type=int, default=304, help="trajectories per GPU")
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--chi", type=int, default=256)
     ap.add_argument("--cutoff", type=float, default=1e-10)
     ap.add_argument("--prefill", type=int, default=4)
     ap.add_argument("--prec", default="df", choices=["df", "mixed", "f64"])
     ap.add_argument("--seed", type=int, default=20261203)
-    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--cpu-seconds", type=float, default=60.0)
     ap.add_argument("--schedule", type=int, default=1, choices=[0, 1])
     ap.add_argument("--scheme", type=int, default=None, choices=[0, 1, 2, 3],
                     help="Jacobi block scheme (default: the library's)")
@@ -199,12 +199,13 @@ def ncu_traffic(prec):
 # ----------------------------------------------------------- CPU (oracle)
 def _ref_traj_worker(args):
     """One trajectory of the benchmark workload with the FP64 oracle on one
-    core: the untimed layers [0, t_first) from |0...0>, then timed layers
-    from t_first on (each apply_bilayer plus its half-chain entropy read)
-    until `budget` seconds have passed, at least one whole layer.  Inputs
-    come from oracle.gen_ref, the GPU arm's generator restated in Python, so
-    this arm loads no library of the product."""
-    root, n, chi, cutoff, seed, traj, p, t_first, budget = args
+    core: the untimed layers [0, t_first) from |0...0>, then the timed
+    layers t_first, t_first + 1, ... (each apply_bilayer plus its half-chain
+    entropy read), whole layers, until `budget` seconds have passed or
+    `layers` layers are done (at least one).  Inputs come from
+    oracle.gen_ref, the GPU arm's generator restated in Python, so this arm
+    loads no library of the product."""
+    root, n, chi, cutoff, seed, traj, p, t_first, budget, layers = args
     os.environ["OPENBLAS_NUM_THREADS"] = "1"
     os.environ["OMP_NUM_THREADS"] = "1"
     if root not in sys.path:
@@ -225,45 +226,57 @@ def _ref_traj_worker(args):
         m.entropy_vn(n // 2 - 1)
         times.append(time.perf_counter() - a0)
         t += 1
-        if time.perf_counter() - start >= budget:
+        if time.perf_counter() - start >= budget or len(times) >= layers:
             break
     return {"traj": traj, "p": p, "prep_s": prep, "layer_s": times,
             "mid_bond_dim": int(len(m.svals[n // 2 - 1]))}
 
 
-def reference_jobs(n, chi, cutoff, seed, t_first, budget, cores):
-    return [(str(ROOT), n, chi, cutoff, seed, i, p_of(i), t_first, budget) for i in range(cores)]
+def reference_jobs(n, chi, cutoff, seed, t_first, budget, cores, layers):
+    return [(str(ROOT), n, chi, cutoff, seed, i, p_of(i), t_first, budget, layers) for i in range(cores)]
 
 
-def summarize_reference(res, t_first, budget):
-    """Throughput of the per-trajectory oracle processes: the sum over
-    processes of timed layers / time."""
+def summarize_reference(res, t_first, budget, layers):
+    """CPU throughput on the GPU arm's workload: every trajectory must run
+    the same `layers` layers from t_first, so the job takes the mean over
+    trajectories of that time per core: throughput = cores * layers / mean
+    T_i.  T_i = the measured whole layers plus, for layers beyond the time
+    budget, the last measured layer's time each (bond dimensions only grow
+    over these layers, so this underestimates the CPU's time: the CPU
+    number is an upper bound)."""
     cores = len(res)
-    rate = sum(len(r["layer_s"]) / sum(r["layer_s"]) for r in res)
-    layers = sum(len(r["layer_s"]) for r in res)
-    mean_layer = statistics.mean(x for r in res for x in r["layer_s"])
+    est = []
+    for r in res:
+        ls = r["layer_s"]
+        est.append(sum(ls) + max(0, layers - len(ls)) * ls[-1])
+    rate = cores * layers / statistics.mean(est)
+    measured = sum(len(r["layer_s"]) for r in res)
     return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": (f"FP64 oracle (numpy + LAPACK gesvd, 1 BLAS thread per process) on {cores} processes; "
                        f"process i runs trajectory i of the GPU batch (p cycling {list(P_LIST)}) from |0...0> "
-                       f"through layers [0, {t_first}) untimed, then times whole layers from layer {t_first} "
-                       f"on for {budget:.0f} s ({layers} traj-layers timed, at least one per process)"),
-            "seconds_per_traj_layer_per_core": mean_layer,
-            "per_process": [{"traj": r["traj"], "p": r["p"], "layers": len(r["layer_s"]),
-                             "mean_layer_s": statistics.mean(r["layer_s"]), "prep_s": r["prep_s"],
-                             "mid_bond_dim": r["mid_bond_dim"]} for r in res]}
+                       f"through layers [0, {t_first}) untimed, then times whole layers of [{t_first}, "
+                       f"{t_first + layers}) for up to {budget:.0f} s ({measured} traj-layers measured, at least one "
+                       f"per process); the layers beyond the budget are counted at the last measured layer's "
+                       f"time (an underestimate of the CPU's time); throughput = cores x {layers} / mean time "
+                       f"per trajectory"),
+            "seconds_per_traj_layer_per_core": statistics.mean(e / layers for e in est),
+            "per_process": [{"traj": r["traj"], "p": r["p"], "layers_measured": len(r["layer_s"]),
+                             "layer_s": r["layer_s"], "estimated_s_for_all_layers": e, "prep_s": r["prep_s"],
+                             "mid_bond_dim": r["mid_bond_dim"]} for r, e in zip(res, est)]}
 
 
-def reference_arm(n, chi, cutoff, seed, t_first, budget, cores):
+def reference_arm(n, chi, cutoff, seed, t_first, budget, cores, layers):
     """The CPU arm on the same workload as the GPU arm: `cores` spawned
     processes (one BLAS thread each, the reference's rayon-over-trajectories
     pattern), process i running batch trajectory i (p cycling) from |0...0>
-    to the GPU arm's first timed layer untimed, then timing whole layers."""
+    to the GPU arm's first timed layer untimed, then timing whole layers of
+    the GPU arm's timed range."""
     import multiprocessing as mp
     os.environ["OPENBLAS_NUM_THREADS"] = "1"
     os.environ["OMP_NUM_THREADS"] = "1"
     with mp.get_context("spawn").Pool(cores) as pool:
-        res = pool.map(_ref_traj_worker, reference_jobs(n, chi, cutoff, seed, t_first, budget, cores))
-    return summarize_reference(res, t_first, budget)
+        res = pool.map(_ref_traj_worker, reference_jobs(n, chi, cutoff, seed, t_first, budget, cores, layers))
+    return summarize_reference(res, t_first, budget, layers)
 
 
 # --------------------------------------------------------------- GPU arm
@@ -777,7 +790,7 @@ def main():
         if rank != 0:
             return
         cores = len(os.sched_getaffinity(0))
-        cb = reference_arm(a.n, a.chi, a.cutoff, a.seed, t_first, a.cpu_seconds, cores)
+        cb = reference_arm(a.n, a.chi, a.cutoff, a.seed, t_first, a.cpu_seconds, cores, a.steps)
         v = cb["value"]
         out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus,
                "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * cb["seconds_per_traj_layer_per_core"],
@@ -788,8 +801,8 @@ def main():
                "per_process": cb["per_process"],
                "note": "the reference is Rust (tensor-net) and no Rust toolchain exists on these machines, so the "
                        "reference arm is its FP64 restatement (oracle/mps_ref.py, LAPACK gesvd as the reference's "
-                       "ndarray-linalg svd_into) on the host cores; a step here is one traj-layer per process "
-                       "(ms_per_step = mean seconds per traj-layer on one core)"}
+                       "ndarray-linalg svd_into) on the host cores; ms_per_step = mean seconds per traj-layer of "
+                       "one core over the timed layers"}
         print(json.dumps(out), flush=True)
         return
 
@@ -815,7 +828,8 @@ def main():
         os.environ["OPENBLAS_NUM_THREADS"] = "1"
         cpu_pool = mp.get_context("spawn").Pool(cores)
         cpu_async = cpu_pool.map_async(_ref_traj_worker,
-                                       reference_jobs(a.n, a.chi, a.cutoff, a.seed, t_first, a.cpu_seconds, cores))
+                                       reference_jobs(a.n, a.chi, a.cutoff, a.seed, t_first, a.cpu_seconds, cores,
+                                                      a.steps))
 
     import torch
     if world > 1:
@@ -875,7 +889,13 @@ def main():
         import __graft_entry__ as ge
         pl = run_plain(a, ge.load_package(), r["plain_states"])
         out["plain_gpu"] = pl
-        out["batched_over_plain"] = r["value"] / pl["value"]
+        # the plain path is timed on the first timed layer, so it is compared with
+        # the batch's rate on that same layer (every later layer costs more)
+        first = r["B"] / (r["step_ms"][0] / 1e3) if r["step_ms"] else None
+        out["batched_first_layer"] = {"value": first, "unit": UNIT, "layer": t_first}
+        out["batched_over_plain"] = first / pl["value"] if first else None
+        out["batched_over_plain_note"] = ("batched rate on layer {0} (the first timed layer) over the plain path on "
+                                          "the same layer").format(t_first)
     if rank == 0 and world == 1 and a.serve_seconds > 0:
         import __graft_entry__ as ge
         out["serving"] = run_serving(a, ge.load_package())
@@ -883,7 +903,7 @@ def main():
         res = cpu_async.get()
         cpu_pool.close()
         cpu_pool.join()
-        cb = summarize_reference(res, t_first, a.cpu_seconds)
+        cb = summarize_reference(res, t_first, a.cpu_seconds, a.steps)
         out["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
         out["cpu_baseline"]["seconds_per_traj_layer_per_core"] = cb["seconds_per_traj_layer_per_core"]
     if rank == 0:

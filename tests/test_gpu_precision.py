@@ -19,6 +19,7 @@ the GPU is in use).
 import json
 import os
 
+import numpy as np
 import pytest
 
 from test_gpu_workloads import P_SET, _compare, _gpu_run, _oracle_run, _pool
@@ -48,3 +49,78 @@ def test_double_float_meets_the_entropy_bound_per_p(pkg):
         c = report[f"df p={p}"]
         assert c["records_equal"], (p, c)
         assert c["entropy_abs"] < 1e-6 and c["prob_abs"] < 1e-6 and c["schmidt_rel"] < 1e-6, (p, c)
+
+
+def _per_layer_errors(ref, gpu):
+    r_ents, _, _ = ref
+    g_ents, _, _ = gpu
+    return [abs(a - b) for a, b in zip(r_ents, g_ents)]
+
+
+def _schmidt_abs(ref_sv, gpu_sv):
+    e = 0.0
+    for a, b in zip(ref_sv, gpu_sv):
+        k = min(len(a), len(b))
+        if k:
+            e = max(e, float(np.max(np.abs(np.asarray(a[:k]) - np.asarray(b[:k])))))
+    return e
+
+
+def _precision_workload(pkg, depth, precs):
+    """The precision workload's own size (N=64, chi_max=256, cutoff 1e-10),
+    one seeded trajectory per p, through `depth` layers: GPU modes against
+    the FP64 oracle."""
+    n, chi, cutoff = 64, 256, 1e-10
+    trajs = [pkg.gen_trajectory(SEED + 1, j, n, depth, p) for j, p in enumerate(P_SET)]
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    with _pool(len(P_SET)) as ex:
+        refs = list(ex.map(_oracle_run, [(root, n, chi, cutoff, t) for t in trajs]))
+    report = {}
+    for prec in precs:
+        b = pkg.Batch([n] * len(trajs), [pkg.Trunc.both(chi, cutoff)] * len(trajs), prec)
+        ents, recs = [[] for _ in trajs], [[] for _ in trajs]
+        for t in range(depth):
+            r, e = b.step(list(range(len(trajs))), [tl[t] for tl in trajs])
+            for i in range(len(trajs)):
+                ents[i].append(float(e[i]))
+                recs[i].append(r[i])
+        svals = [[b.svals(i, bd) for bd in range(n - 1)] for i in range(len(trajs))]
+        report[f"{prec} device_status"] = b.device_status()
+        b.close()
+        for j, p in enumerate(P_SET):
+            c = _compare(refs[j], (ents[j], recs[j], svals[j]), floor=1e-6 if prec != "mixed" else 1e-4)
+            c["schmidt_abs"] = _schmidt_abs(refs[j][2], svals[j])
+            c["entropy_abs_per_layer"] = _per_layer_errors(refs[j], (ents[j], recs[j], svals[j]))
+            c["middle_bond_dim_at_end"] = int(len(refs[j][2][n // 2 - 1]))
+            report[f"{prec} p={p}"] = c
+    return dict(workload=dict(n=n, chi_max=chi, cutoff=cutoff, depth=depth, seed=SEED + 1, trajectories_per_p=1),
+                errors=report)
+
+
+def test_double_float_at_the_precision_workload_size(pkg):
+    """The first layers of the precision workload at its full size (N=64,
+    chi_max=256, cutoff 1e-10), where the oracle finishes in seconds: the DF
+    path within 1e-6 of the oracle on entropies and probabilities, identical
+    outcome records, Schmidt values to 1e-6 relative above 1e-6."""
+    rep = _precision_workload(pkg, 8, ("df",))
+    assert rep["errors"]["df device_status"] == 0
+    for p in P_SET:
+        c = rep["errors"][f"df p={p}"]
+        assert c["records_equal"], (p, c)
+        assert c["entropy_abs"] < 1e-6 and c["prob_abs"] < 1e-6 and c["schmidt_rel"] < 1e-6, (p, c)
+
+
+@pytest.mark.skipif(not os.environ.get("TN_PRECISION_WORKLOAD_DEPTH"),
+                    reason="deep report of the precision workload: set TN_PRECISION_WORKLOAD_DEPTH (minutes of oracle time)")
+def test_precision_workload_report(pkg):
+    """The precision workload at N=64, chi_max=256 through
+    $TN_PRECISION_WORKLOAD_DEPTH layers, DF and MIXED against the oracle, the
+    report written to $TN_PRECISION_REPORT; DF is held to 1e-6."""
+    rep = _precision_workload(pkg, int(os.environ["TN_PRECISION_WORKLOAD_DEPTH"]), ("df", "mixed"))
+    out = os.environ.get("TN_PRECISION_REPORT")
+    if out:
+        with open(out, "w") as f:
+            json.dump(rep, f, indent=1)
+    for p in P_SET:
+        c = rep["errors"][f"df p={p}"]
+        assert c["records_equal"] and c["entropy_abs"] < 1e-6, (p, c)
