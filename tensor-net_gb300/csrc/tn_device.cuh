@@ -1327,11 +1327,16 @@ __device__ __forceinline__ dd dd_cabs(cpx<dd> g, cpx<dd> *phase) {
   return mx * r;
 }
 
+// |g| / sqrt(a b) of a double-float Gram pair, divided step by step to stay
+// in range; 0 when either diagonal is at the noise level.
+__device__ __forceinline__ dd pair_ratio(dd a, dd b, cpx<dd> g, dd tiny2) {
+  if (!(a > tiny2 && b > tiny2)) return dd(0.f, 0.f);
+  return (dd_cabs(g, nullptr) / sqrt(a)) / sqrt(b);
+}
+
 template <>
 __device__ __forceinline__ bool pair_active<dd>(dd a, dd b, cpx<dd> g, dd tol, dd tiny2) {
-  if (!(a > tiny2 && b > tiny2)) return false;
-  // |g| / sqrt(a) / sqrt(b) > tol, divided step by step to stay in range
-  return (dd_cabs(g, nullptr) / sqrt(a)) / sqrt(b) > tol;
+  return pair_ratio(a, b, g, tiny2) > tol;
 }
 
 // The double-float rotation: the formulas of the generic version, with |g|
@@ -1499,9 +1504,20 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
   // Double-float: the sweeps start guided (float Gram of the hi parts, float
   // rotation angles, double-float rotations and update) until a sweep finds
   // no pair above the float threshold; the last sweeps run in double-float.
+  //
+  // Cyclic Jacobi converges quadratically near the end: a sweep whose pairs
+  // all had |g| <= r sqrt(a b) before their rotations leaves pairs of order
+  // r^2 / (relative gap).  So a guided sweep with every pair below
+  // kGuidedDone (1e-4: the next guided sweep would find ~1e-8 / gap, under
+  // the float threshold ~5e-6) hands over to double-float at once instead of
+  // running one more float Gram only to find nothing, and a double-float sweep with
+  // every pair below kFinishDone (1e-9: what is left is ~1e-18 / gap, under
+  // the double-float threshold tol ~6e-13 for relative gaps down to 1e-5)
+  // is the last one, instead of a further Gram pass that only confirms it.
   constexpr bool kDD = std::is_same<T, dd>::value;
   bool guided = kDD;
   const float tol_f = 4.f * sqrtf(float(ell)) * Eps<float>::v;
+  constexpr float kGuidedDone = 1e-4f, kFinishDone = 1e-9f;
   // Columns with |a|^2 <= eps^2 ||A||_F^2 are rounding noise: rotating them
   // changes nothing above rounding and their relative off-diagonals never
   // settle, so they are neither rotated nor counted for convergence.
@@ -1549,6 +1565,7 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
   };
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     int rotated = 0;
+    int far = 0;  // (double-float) some pair of this sweep above kGuidedDone / kFinishDone
     if (nblk > 2) {
       flush();  // the re-ordering changes which columns a block id names
       int P = 1;
@@ -1658,7 +1675,7 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
       // converged rotates only the cross pairs (H rounds instead of W-1), and
       // vice versa; a sweep still ends only when no pair of any step needs a
       // rotation, so convergence is decided on every pair as before.
-      int needW = 0, needC = 0;
+      int needW = 0, needC = 0, farS = 0;
       for (int idx = threadIdx.x; idx < W * W; idx += NT) {
         int p = idx / W, q = idx % W;
         if (p < q && cols[p] >= 0 && cols[q] >= 0) {
@@ -1668,10 +1685,18 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
           bool act;
           if (kDD && guided) {
             const cpx<float> *Gf = reinterpret_cast<const cpx<float> *>(sm.G);
-            act = pair_active<float>(Gf[p * (W + 1) + p].x, Gf[q * (W + 1) + q].x, Gf[p * (W + 1) + q], tol_f,
-                                     tiny2_f);
+            const float a = Gf[p * (W + 1) + p].x, b = Gf[q * (W + 1) + q].x;
+            act = pair_active<float>(a, b, Gf[p * (W + 1) + q], tol_f, tiny2_f);
+            farS |= int(pair_active<float>(a, b, Gf[p * (W + 1) + q], kGuidedDone, tiny2_f));
           } else {
-            act = pair_active<T>(sm.G[p * (W + 1) + p].x, sm.G[q * (W + 1) + q].x, sm.G[p * (W + 1) + q], tol, tiny2);
+            if constexpr (kDD) {
+              const dd r = pair_ratio(sm.G[p * (W + 1) + p].x, sm.G[q * (W + 1) + q].x, sm.G[p * (W + 1) + q], tiny2);
+              act = r > tol;
+              farS |= int(r.hi > kFinishDone);
+            } else {
+              act = pair_active<T>(sm.G[p * (W + 1) + p].x, sm.G[q * (W + 1) + q].x, sm.G[p * (W + 1) + q], tol,
+                                   tiny2);
+            }
           }
           if (act) {
             if (cross)
@@ -1683,6 +1708,7 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
       }
       needW = __syncthreads_or(needW);
       needC = __syncthreads_or(needC);
+      if constexpr (kDD) far |= __syncthreads_or(farS);
       const int need = needW | needC;
       if (mode == 0 && !(needW && needC)) mode = needC ? 1 : 2;
       long long t1 = clock64();
@@ -1753,7 +1779,7 @@ __device__ int jacobi_svd(cpx<T> *__restrict__ A, int ell, int c, int max_sweeps
         cyc[2] += clock64() - t1;
       }
     }
-    if (!rotated) {
+    if (!rotated || (kDD && !far)) {
       if (guided) {  // float-converged: the remaining sweeps in double-float
         guided = false;
         continue;
