@@ -9,13 +9,14 @@ for every implementation).  The batch first evolves `--prefill` layers
 untimed from |0...0> so that the timed layers run in the entangled regime.
 
 Lines printed (rank 0): one JSON object per run.
-  value     traj-layers/s with the layer inputs already in HBM (device
-            pointers, one persistent launch per layer), CUDA events on the
-            batch stream, max over ranks;
-  e2e       the same timed layers from the same state (a second batch
-            replays the untimed layers) through the C ABI (tn_batch_step) with
-            host buffers: pinned H2D of the layer inputs and D2H of
-            outcomes/probabilities/entropies inside the timed region;
+  value     traj-layers/s from the device time of each timed layer between
+            its input copy and its output copy (CUDA events on the batch
+            stream around the layer's kernels: inputs resident in HBM), max
+            over ranks;
+  e2e       the same timed layers (the same calls) timed on the host: each
+            layer through the C ABI (tn_batch_step) with host buffers, the
+            pinned H2D of its inputs and the D2H of its outcomes,
+            probabilities and entropies inside the timed region;
   roofline  algorithmic flops (theta GEMM + Golub-Reinsch SVD count of every
             bond operation, counted on the device) per launch / launch time;
   cpu_baseline  the FP64 oracle (numpy + LAPACK gesvd) on the host cores on a
@@ -63,9 +64,10 @@ def parse():
                     help="Jacobi block scheme (default: the library's)")
     ap.add_argument("--runs", type=int, default=64, help="coev: sampled trajectories")
     ap.add_argument("--workload", default="batch", choices=["batch", "mixed", "large", "precision", "coev", "plain",
-                                                                 "f64"],
+                                                                 "f64", "vsplain"],
                     help="batch: the headline line; mixed: the batching workload; large: n=128, chi_max=1024; "
-                         "precision: mixed vs float64 errors per p (uses --n, --chi, --depth)")
+                         "precision: mixed vs float64 errors per p (uses --n, --chi, --depth); vsplain: batched vs "
+                         "plain on layer --prefill + 1 in --prec")
     ap.add_argument("--depth", type=int, default=64)
     ap.add_argument("--theta", default="tc", choices=["tc", "simt"],
                     help="mixed precision theta contraction: tensor cores (tcgen05) or SIMT FP32")
@@ -689,6 +691,60 @@ def run_f64(a):
             "note": "host-timed, inputs through tn_batch_step (e2e); plain = one p=0.10 trajectory"}
 
 
+def run_vs_plain(a):
+    """Batched vs plain on one layer of the headline workload (N=64,
+    chi_max=256, p cycling) in `--prec`: `--batch` trajectories step through
+    layers [0, --prefill] (the last one as warm-up), then layer --prefill + 1
+    is timed through tn_batch_step with host buffers.  Trajectories 0..4 (one
+    per p) continue from the states they had in the batch before that layer
+    (checkpoint export / import) through the single-state API, one traj-layer
+    each with its entropy read, host-timed: both sides run the same layer of
+    the same trajectories."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    n, chi, B = a.n, a.chi, a.batch
+    trunc = pkg.Trunc.both(chi, a.cutoff)
+    batch = pkg.Batch([n] * B, [trunc] * B, a.prec)
+    trajs = list(range(B))
+
+    def lay(t):
+        return [pkg.gen_layer(a.seed, i, t, n, p_of(i)) for i in trajs]
+
+    for t in range(a.prefill + 1):
+        batch.step(trajs, lay(t))
+    t_lo = a.prefill + 1
+    states = [batch.export_parts(i) for i in range(min(len(P_LIST), B))]
+    pk = batch.pack(trajs, lay(t_lo))
+    batch.synchronize()
+    t0 = time.perf_counter()
+    batch.step_packed(pk)
+    b_s = time.perf_counter() - t0
+    status = batch.device_status()
+    dims = [int(batch.bond_dims(i)[n // 2 - 1]) for i in range(len(states))]
+    batch.close()
+    plain_s = []
+    for i, (gammas, lams) in enumerate(states):
+        m = pkg.MPS.from_parts(gammas, lams, trunc, a.prec, chi)
+        m.entropy_vn(n // 2 - 1)
+        inp = pkg.gen_layer(a.seed, i, t_lo, n, p_of(i))
+        t0 = time.perf_counter()
+        m.apply_bilayer(*inp)
+        m.entropy_vn(n // 2 - 1)  # the layer's entropy read (synchronises)
+        plain_s.append(time.perf_counter() - t0)
+        m.close()
+    batched = B / b_s
+    plain = len(plain_s) / sum(plain_s)
+    return {"workload": f"N={n} chi_max={chi} cutoff={a.cutoff:g} {a.prec}, {B} trajectories (p cycling "
+                        f"{list(P_LIST)}), layer {t_lo} after {t_lo} untimed layers",
+            "batched": {"value": batched, "unit": UNIT, "layer_s": b_s, "device_status": status},
+            "plain": {"value": plain, "unit": UNIT, "traj_layer_s": dict(zip([str(p_of(i)) for i in range(len(plain_s))],
+                                                                             plain_s)),
+                      "how": "trajectories 0..4 (one per p) from their batch states, single-state API"},
+            "middle_bond_dims_after": dims,
+            "batched_over_plain": batched / plain,
+            "note": "host-timed on both sides (batched: tn_batch_step with pinned H2D and D2H)"}
+
+
 def run_coev(a):
     """The multi-chi coevolution replay (the reference's production driver,
     workspace/src/haar_coev_probs.rs): `--runs` sampled trajectories of one
@@ -809,13 +865,13 @@ def main():
         print(json.dumps(out), flush=True)
         return
 
-    if a.workload in ("mixed", "large", "precision", "coev", "plain", "f64"):
+    if a.workload in ("mixed", "large", "precision", "coev", "plain", "f64", "vsplain"):
         if rank != 0:
             return
         import torch
         torch.cuda.set_device(0)
         out = {"mixed": run_mixed, "large": run_large, "precision": run_precision, "coev": run_coev,
-               "plain": run_plain_small, "f64": run_f64}[a.workload](a)
+               "plain": run_plain_small, "f64": run_f64, "vsplain": run_vs_plain}[a.workload](a)
         out.update({"metric": METRIC if a.workload == "mixed" else "per-layer time and entropy",
                     "n_gpus": 1, "data": "synthetic (seeded Haar gates and measurement uniforms)"})
         print(json.dumps(out), flush=True)
