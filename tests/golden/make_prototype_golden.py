@@ -13,6 +13,12 @@ oracle to code the reference ships.
 * gate2: n = 2 only, ``apply_2q(canonicalize(2, psi), 0, U)``: the Schmidt
   values after a Haar gate.  (The prototype's ``apply_2q`` leaves out the
   outer Lambdas of theta, which is exact only for two qubits.)
+* gate1: ``apply_1q`` of a one-qubit Haar gate on one site (exact for any n):
+  the contracted state.
+* proj: ``project(mps, k, p)`` where the prototype's contraction spans the
+  whole chain (n = 2; the middle site of n = 3): Schmidt values and state
+  (the middle-site branch's state does not contract back to the projected
+  vector; its Schmidt values are right).
 
 haar-unitary.py plots at import time and imports a plotting package that is
 not installed, so only its ``random_haar`` definition is compiled (taken from
@@ -100,6 +106,33 @@ def main():
         out[f"gate2_{i}_u"] = u
         out[f"gate2_{i}_L"] = np.asarray(mps.L[0], dtype=np.float64)
         out[f"gate2_{i}_contract"] = np.asarray(sm.contract(mps), dtype=np.complex128)
+    # gate1: a one-qubit Haar gate (random_haar(1)) on one site of a longer
+    # chain; apply_1q acts on one Gamma, which is exact for any n
+    for i, (n, k) in enumerate([(3, 1), (5, 0), (5, 2), (6, 5)]):
+        psi = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+        psi /= np.linalg.norm(psi)
+        np.random.seed(9400 + i)
+        u = np.asarray(random_haar(1), dtype=np.complex128)
+        mps = sm.canonicalize(n, psi.copy())
+        sm.apply_1q(mps, k, u)
+        out[f"gate1_{i}_nk"] = np.array([n, k])
+        out[f"gate1_{i}_psi"] = psi
+        out[f"gate1_{i}_u"] = u
+        out[f"gate1_{i}_contract"] = np.asarray(sm.contract(mps), dtype=np.complex128)
+
+    # proj: projection of site k onto outcome p; the prototype's project
+    # contracts the sites around k without the outer Lambdas, which is exact
+    # when those sites are the whole chain (n = 2, and the middle site of n = 3)
+    for i, (n, k, p) in enumerate([(2, 0, 0), (2, 0, 1), (2, 1, 0), (2, 1, 1), (3, 1, 0), (3, 1, 1)]):
+        psi = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+        psi /= np.linalg.norm(psi)
+        mps = sm.canonicalize(n, psi.copy())
+        sm.project(mps, k, p)
+        out[f"proj_{i}_nkp"] = np.array([n, k, p])
+        out[f"proj_{i}_psi"] = psi
+        for b, s in enumerate(mps.L):
+            out[f"proj_{i}_L{b}"] = np.asarray(s, dtype=np.float64)
+        out[f"proj_{i}_contract"] = np.asarray(sm.contract(mps), dtype=np.complex128)
     np.savez_compressed(OUT, **out)
     print(f"wrote {OUT} ({len(out)} arrays)")
 
