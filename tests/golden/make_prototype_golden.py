@@ -15,6 +15,8 @@ oracle to code the reference ships.
   outer Lambdas of theta, which is exact only for two qubits.)
 * gate1: ``apply_1q`` of a one-qubit Haar gate on one site (exact for any n):
   the contracted state.
+* entropy: ``entropy_log`` of the reduced density matrix (``trace_qubit``)
+  from prototyping/entropy.py, for every bond of the n = 4, 6, 8 states.
 * proj: ``project(mps, k, p)`` where the prototype's contraction spans the
   whole chain (n = 2; the middle site of n = 3): Schmidt values and state
   (the middle-site branch's state does not contract back to the projected
@@ -45,6 +47,15 @@ def _random_haar():
     ns = {"np": np}
     exec(compile(mod, str(PROTO / "haar-unitary.py"), "exec"), ns)
     return ns["random_haar"]
+
+
+def _defs(fname, names, ns):
+    """Compile only the named top-level definitions of a prototype script
+    (the scripts print or plot at import time)."""
+    src = (PROTO / fname).read_text()
+    body = [n for n in ast.parse(src).body if isinstance(n, ast.FunctionDef) and n.name in names]
+    exec(compile(ast.Module(body=body, type_ignores=[]), str(PROTO / fname), "exec"), ns)
+    return ns
 
 
 def _schmidt_mps():
@@ -133,6 +144,21 @@ def main():
         for b, s in enumerate(mps.L):
             out[f"proj_{i}_L{b}"] = np.asarray(s, dtype=np.float64)
         out[f"proj_{i}_contract"] = np.asarray(sm.contract(mps), dtype=np.complex128)
+    # entropy: -tr(rho log rho) of the left part (qubits 0..b) of the seeded
+    # states above, by entropy.py's trace_qubit / entropy_log
+    from scipy.linalg import logm
+    ent = _defs("entropy.py", {"trace", "trace_qubit", "entropy_log"}, {"np": np, "logm": logm})
+    for n in (4, 6, 8):
+        psi = out[f"schmidt_n{n}_psi"]
+        rho = np.outer(psi, psi.conj())
+        red = rho
+        ents = np.zeros(n - 1)
+        for m in range(n, 0, -1):  # red: the density matrix of qubits 0..m-1
+            if m <= n - 1:  # bond m - 1 separates qubits 0..m-1 from the rest
+                ents[m - 1] = float(np.real(ent["entropy_log"](red)))
+            if m > 1:
+                red = ent["trace_qubit"](m, m - 1, red)
+        out[f"entropy_n{n}"] = ents
     np.savez_compressed(OUT, **out)
     print(f"wrote {OUT} ({len(out)} arrays)")
 

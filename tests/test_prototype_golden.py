@@ -2,10 +2,11 @@
 
 tests/golden/prototype.npz was written by tests/golden/make_prototype_golden.py
 from the reference tree's prototyping/haar-unitary.py (``random_haar``) and
-prototyping/schmidt_mps.py (``canonicalize``, ``contract``, ``apply_2q``),
-run on seeded inputs.  These are the only parts of the reference that run
-here (the library is Rust), so they pin three pieces of the oracle to code
-the reference ships:
+prototyping/schmidt_mps.py (``canonicalize``, ``contract``, ``apply_1q``,
+``apply_2q``, ``project``) and prototyping/entropy.py (``trace_qubit``,
+``entropy_log``), run on seeded inputs.  These are the only parts of the
+reference that run here (the library is Rust), so they pin these pieces of
+the oracle to code the reference ships:
 
 * the Haar recipe of ``gate::haar`` (gate.rs:888-909): the oracle's numpy
   form and the restatement of the C++ input generator's Gram-Schmidt form
@@ -16,6 +17,8 @@ the reference ships:
   ``apply_2q``, which leaves the outer Lambdas out of theta, is exact): the
   Schmidt values and the state after ``apply_unitary2``;
 * ``apply_unitary1`` (mps.rs:1298-1314) against ``apply_1q``: the state;
+* ``entropy_vn`` against ``entropy_log`` of the reduced density matrix
+  (prototyping/entropy.py's ``trace_qubit``) on every bond;
 * ``local_prob`` + ``project`` + the refactor sweep of
   ``measure_postsel_prob`` (mps.rs:1079-1134, 1453-1465, 1501-1510) against
   ``project`` where the prototype's contraction spans the whole chain (n = 2,
@@ -108,3 +111,12 @@ def test_projection_matches_project():
         for b in range(n - 1):
             ref = _above(G[f"proj_{i}_L{b}"])
             np.testing.assert_allclose(_above(m.svals[b]), ref, rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("n", [4, 6, 8])
+def test_entropy_matches_the_reduced_density_matrix(n):
+    """entropy_vn (mps.rs:1251-1261) on every bond against -tr(rho log rho) of
+    the reduced density matrix, by the reference's prototyping/entropy.py."""
+    m = mps_ref.from_vector(G[f"schmidt_n{n}_psi"])
+    got = np.array([m.entropy_vn(b) for b in range(n - 1)])
+    np.testing.assert_allclose(got, G[f"entropy_n{n}"], rtol=0, atol=1e-12)
